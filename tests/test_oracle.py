@@ -1,0 +1,120 @@
+"""The CPU oracle pinned against fixtures produced by the reference's own
+cluster_with_cpu (src/dbscan/util.cpp:299-354) and, where the reference tree is
+present, against that code run live on fresh seeded inputs."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden_files, load_golden
+
+import oracle as O
+from rtdbstream_gb300 import workloads as wl
+
+
+def _nonnoise_equal(lab, cid_a, cid_b):
+    keep = lab != 2
+    return np.array_equal(cid_a[keep], cid_b[keep])
+
+
+@pytest.mark.parametrize("path", golden_files("window"), ids=os.path.basename)
+def test_window_grid_fp32_matches_reference_golden(oracle_lib, path):
+    g = load_golden(path)
+    nn, lab, cid, _ = O.window_grid(g["pts"], float(g["eps"]), int(g["min_pts"]), O.MODE_FP32)
+    assert np.array_equal(nn, g["nn"])
+    assert np.array_equal(lab, g["label"])
+    assert _nonnoise_equal(lab, cid, g["cid"])
+    assert np.array_equal(cid[lab == 2], np.nonzero(lab == 2)[0])
+
+
+@pytest.mark.parametrize("path", golden_files("window"), ids=os.path.basename)
+def test_window_bruteforce_restatement_matches_reference_golden(oracle_lib, path):
+    g = load_golden(path)
+    nn, lab, cid = O.window_bruteforce(g["pts"], float(g["eps"]), int(g["min_pts"]))
+    assert np.array_equal(nn, g["nn"])
+    assert np.array_equal(lab, g["label"])
+    assert _nonnoise_equal(lab, cid, g["cid"])
+
+
+@pytest.mark.parametrize("path", golden_files("stream"), ids=os.path.basename)
+def test_stream_fp32_matches_reference_golden(oracle_lib, path):
+    g = load_golden(path)
+    W, S = int(g["W"]), int(g["S"])
+    slides = g["nn"].shape[0]
+    nn, lab, cid = O.stream(g["pts"], W, S, float(g["eps"]), int(g["min_pts"]), O.MODE_FP32,
+                            first_slide=1, n_out=slides)
+    assert np.array_equal(nn, g["nn"])
+    assert np.array_equal(lab, g["label"])
+    for k in range(slides):
+        assert _nonnoise_equal(lab[k], cid[k], g["cid"][k])
+
+
+@pytest.mark.parametrize("path", golden_files("window"), ids=os.path.basename)
+def test_fp64_mode_agrees_outside_band(oracle_lib, path):
+    """FP64 and the reference's FP32 predicate may disagree only on pairs whose
+    FP32 squared distance lies inside the re-check band."""
+    g = load_golden(path)
+    eps, mp = float(g["eps"]), int(g["min_pts"])
+    nn64, lab64, cid64, st = O.window_grid(g["pts"], eps, mp, O.MODE_FP64)
+    if st["band_pairs"] == 0:
+        assert np.array_equal(nn64, g["nn"])
+        assert np.array_equal(lab64, g["label"])
+        assert _nonnoise_equal(lab64, cid64, g["cid"])
+    else:
+        # every count difference is bounded by the number of band pairs
+        assert np.abs(nn64 - g["nn"]).sum() <= 2 * st["band_pairs"]
+
+
+def test_band_pairs_present_in_precision_fixture(oracle_lib):
+    g = load_golden(os.path.join(os.path.dirname(golden_files("window")[0]), "band3d_w3000.npz"))
+    nn64, _, _, st = O.window_grid(g["pts"], float(g["eps"]), int(g["min_pts"]), O.MODE_FP64)
+    assert st["band_pairs"] > 0
+    assert not np.array_equal(nn64, g["nn"])  # FP64 really decides differently there
+
+
+def test_fp64_predicate_is_exact_double_compare(oracle_lib):
+    """Brute-force double evaluation reproduces the FP64-mode counts."""
+    pts = wl.offset_band_points(1500, 1e-3, partner_frac=0.3, seed=5)
+    nn64, _, _, _ = O.window_grid(pts, 1e-3, 2, O.MODE_FP64)
+    p = pts.astype(np.float64)
+    d = p[:, None, :] - p[None, :, :]
+    d2 = (d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2]
+    ref = (d2 < 1e-3 * 1e-3).sum(axis=1)
+    assert np.array_equal(nn64, ref.astype(np.int32))
+
+
+def test_band_bounds():
+    lo, hi, ok = O.band(1e-3)
+    E = 1e-6
+    assert ok and np.float32(lo) < E < np.float32(hi)
+    assert (hi - lo) / E < 4e-6
+    _, _, ok_tiny = O.band(1e-60)
+    assert not ok_tiny
+
+
+@pytest.mark.skipif(O.ref_lib() is None and not os.path.isdir(O.REFERENCE_TREE),
+                    reason="reference tree not present")
+@pytest.mark.parametrize("dim,seed", [(1, 31), (2, 32), (3, 33)])
+def test_live_reference_vs_restatement(oracle_lib, dim, seed):
+    pts = wl.gaussian_mixture(1500, dim=dim, k=6, box=12.0, seed=seed)
+    eps, mp = 0.45, 5
+    a = O.window_reference(pts, eps, mp)
+    b = O.window_grid(pts, eps, mp, O.MODE_FP32)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert _nonnoise_equal(a[1], a[2], b[2])
+
+
+def test_stream_slot_semantics(oracle_lib):
+    """Slide k holds stream points [k*S, k*S+W) at ring slot t mod W."""
+    pts = wl.gaussian_mixture(900, dim=2, k=4, box=10.0, seed=3)
+    W, S = 300, 100
+    nn, lab, cid = O.stream(pts, W, S, 0.5, 4, O.MODE_FP64, first_slide=2, n_out=3)
+    for j, k in enumerate(range(2, 5)):
+        win = O.window_of(pts, W, S, k)
+        nn1, lab1, cid1, _ = O.window_grid(win, 0.5, 4, O.MODE_FP64)
+        assert np.array_equal(nn[j], nn1) and np.array_equal(lab[j], lab1) and np.array_equal(cid[j], cid1)
+
+
+def test_stream_rejects_bad_stride(oracle_lib):
+    with pytest.raises(RuntimeError):
+        O.stream(np.zeros((100, 2), np.float32), 30, 7, 0.5, 3)
