@@ -1,0 +1,187 @@
+/*
+ * rtdbs.h -- C ABI of the GB300-native streaming DBSCAN engine.
+ *
+ * Drop-in for the per-slide clustering path of RTDBStream (level-9 driver,
+ * src/dbscan/dbscan.cpp:2258-2364): a ring-buffer window of W points slides
+ * by S points per step; after every slide the engine returns, indexed by ring
+ * slot, label[W] (0 core, 1 border, 2 noise; src/dbscan/dbscan.h:27) and
+ * cluster_id[W].
+ *
+ * Semantics (identical to the reference's CPU checker cluster_with_cpu,
+ * src/dbscan/util.cpp:299-354, under RTDBS_PREC_FP32):
+ *   - neighbour: squared distance strictly below Eps^2, the point itself
+ *     included; core <=> neighbour count >= min_pts;
+ *   - core id: the minimum core slot of its connected component;
+ *   - border id: the minimum core id over the clusters of its Eps-adjacent
+ *     cores; noise id: its own slot.
+ * Precision modes:
+ *   RTDBS_PREC_FP64 (default) -- the neighbour relation of an FP64
+ *       evaluation of the float32 inputs against Eps*Eps in double; FP32
+ *       filter, pairs inside a proven rounding band re-decided in FP64;
+ *   RTDBS_PREC_FP32 -- the reference's FP32 predicate (float differences and
+ *       squares, compared with (float)Eps*(float)Eps), bit-identical to
+ *       cluster_with_cpu.
+ *
+ * Every function returns an int status (0 = RTDBS_OK, negative = error) and
+ * never throws.  One engine is driven by one host thread at a time; all device
+ * work runs on the engine's CUDA stream.  The engine owns its device memory;
+ * the caller owns its input/output buffers.  No torch types cross this ABI.
+ */
+#ifndef RTDBS_H
+#define RTDBS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RTDBS_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define RTDBS_API __attribute__((visibility("default")))
+#else
+#define RTDBS_API
+#endif
+
+/* Status codes. */
+#define RTDBS_OK             0
+#define RTDBS_ERR_INVALID   -1  /* bad argument: dim not in 1..3, W % S != 0, Eps <= 0, NULL pointer */
+#define RTDBS_ERR_CUDA      -2  /* a CUDA runtime call failed (rtdbs_last_error has the text) */
+#define RTDBS_ERR_OOM       -3  /* device or pinned allocation failed */
+#define RTDBS_ERR_STATE     -4  /* call out of order (slide before rtdbs_load_window) */
+#define RTDBS_ERR_DEVICE    -5  /* a device-side bound was hit (hash probe, union-find retry,
+                                   work-list capacity); the engine must be reloaded */
+#define RTDBS_ERR_NO_DEVICE -6  /* no CUDA device / library built without one */
+
+/* Precision modes. */
+#define RTDBS_PREC_FP64 0
+#define RTDBS_PREC_FP32 1
+
+/* Labels (src/dbscan/dbscan.h:27). */
+#define RTDBS_LABEL_CORE   0
+#define RTDBS_LABEL_BORDER 1
+#define RTDBS_LABEL_NOISE  2
+
+/* Flags of rtdbs_params.flags. */
+#define RTDBS_FLAG_NO_GRAPH 1   /* launch kernels directly instead of replaying a CUDA graph */
+
+/* Engine parameters: the reference's -W -S -R -K arguments
+ * (src/dbscan/util.cpp:454-500) plus the dataset bounding box it derives from
+ * the whole input file (src/dbscan/util.cpp:12-254, used for its grid at
+ * src/dbscan/dbscan.cpp:34-37). */
+typedef struct rtdbs_params {
+    int32_t dim;          /* point dimension, 1..3 */
+    int32_t window;       /* W: points in the window (ring slots) */
+    int32_t stride;       /* S: points entering and leaving per slide; W % S == 0 */
+    int32_t min_pts;      /* MinPts */
+    double  eps;          /* Eps (> 0) */
+    int32_t precision;    /* RTDBS_PREC_* */
+    int32_t has_bbox;     /* 1: bbox_min/bbox_max bound the whole stream; 0: taken from
+                             the first window with a margin (points outside are still
+                             handled exactly, only more slowly) */
+    float   bbox_min[3];
+    float   bbox_max[3];
+    int32_t device;       /* CUDA device ordinal */
+    int32_t flags;        /* RTDBS_FLAG_* */
+    int32_t reserved[6];
+} rtdbs_params;
+
+/* Cumulative counters (src/dbscan/dbscan.cpp:145-212 keeps similar debug counters). */
+typedef struct rtdbs_stats {
+    int64_t slides;          /* slides completed */
+    int64_t band_rechecks;   /* pair tests re-decided in FP64 (FP64 mode) */
+    int64_t cells;           /* non-empty grid cells of the current window */
+    int64_t work_items;      /* cell runs scheduled by the clustering kernels */
+    int32_t error_bits;      /* device error word (0 = healthy) */
+    int32_t key_bits;        /* bits of the cell key */
+    double  cell_side;       /* grid cell side (>= Eps) */
+    int64_t device_bytes;    /* device memory owned by the engine */
+    int32_t launches_per_slide; /* kernels launched by one slide */
+    int32_t chunks_per_slide;   /* grid-update chunks per slide (ceil(S / 16384)) */
+    int64_t reserved[3];
+} rtdbs_stats;
+
+/* Per-phase device time of one profiled slide, in milliseconds (the
+ * reference's Timer phases, src/dbscan/timer.h:10-238, measured with CUDA
+ * events on the engine's stream).  Chunk phases are summed over chunks. */
+typedef struct rtdbs_phase_times {
+    float ingest_ms;      /* new points -> ring slots, cell keys */
+    float sort_ms;        /* radix sort of the chunk's (cell, slot) words */
+    float decrement_ms;   /* -1 on neighbours of expired points */
+    float merge_ms;       /* sorted-window merge */
+    float build_ms;       /* cell table + work list */
+    float increment_ms;   /* counts of new points, +1 on their neighbours */
+    float union_ms;       /* union-find over core pairs */
+    float label_ms;       /* labels, ids, border rule */
+    float total_ms;       /* first launch to last */
+    int32_t chunks;
+} rtdbs_phase_times;
+
+typedef struct rtdbs_engine rtdbs_engine;
+
+RTDBS_API int rtdbs_abi_version(void);
+RTDBS_API const char* rtdbs_status_string(int status);
+/* Text of the last error raised on the calling thread ("" if none). */
+RTDBS_API const char* rtdbs_last_error(void);
+
+/* Fills defaults: dim 3, precision FP64, no bbox, device 0, min_pts 5. */
+RTDBS_API int rtdbs_params_init(rtdbs_params* params);
+
+/* Allocates every device buffer up front, sized by W and S.
+ * Replaces initialize_params (src/dbscan/dbscan.cpp:30-132).
+ * cuda_stream is a cudaStream_t (NULL: the engine creates its own stream). */
+RTDBS_API int rtdbs_create(const rtdbs_params* params, void* cuda_stream, rtdbs_engine** out);
+
+/* Frees everything.  Replaces cleanup (src/dbscan/dbscan.cpp:2366-2448). */
+RTDBS_API int rtdbs_destroy(rtdbs_engine* engine);
+
+/* Loads the first window: points[W][dim] into slots 0..W-1, grid built.
+ * Replaces the first-window set-up (src/dbscan/dbscan.cpp:2268-2272).
+ * points_on_device: 1 if points is a device pointer.  Synchronous. */
+RTDBS_API int rtdbs_load_window(rtdbs_engine* engine, const float* points, int points_on_device);
+
+/* One slide with host buffers: new_points[S][dim] replace slots
+ * [u*S, u*S+S) (u = slides done mod W/S), then label[W] and cluster_id[W]
+ * (host memory; pinned memory avoids a staging copy) receive the window's
+ * result.  Replaces one iteration of the reference's slide loop
+ * (src/dbscan/dbscan.cpp:2276-2362: H2D at 2289, grid update 2293, core
+ * identification 2300-2322, clustering 2331-2336, D2H 2344-2345).
+ * Synchronous; returns RTDBS_ERR_DEVICE if a device bound was hit. */
+RTDBS_API int rtdbs_slide(rtdbs_engine* engine, const float* new_points, int32_t* label,
+                int32_t* cluster_id);
+
+/* Same slide with device pointers, stream-ordered, no host synchronisation.
+ * label/cluster_id may be NULL: the result then stays in the engine's own
+ * buffers (rtdbs_device_outputs). */
+RTDBS_API int rtdbs_slide_async(rtdbs_engine* engine, const float* d_new_points, int32_t* d_label,
+                      int32_t* d_cluster_id);
+
+/* Waits for the engine's stream; reports RTDBS_ERR_DEVICE if a device bound
+ * was hit by any work since the previous check. */
+RTDBS_API int rtdbs_sync(rtdbs_engine* engine);
+
+/* Clusters the current window without sliding (e.g. right after
+ * rtdbs_load_window).  Outputs are host or device memory per on_device. */
+RTDBS_API int rtdbs_cluster(rtdbs_engine* engine, int32_t* label, int32_t* cluster_id, int on_device);
+
+/* Exact neighbour counts (self included) of the current window by slot; the
+ * reference's nn / check_nn (src/dbscan/util.cpp:299-323). */
+RTDBS_API int rtdbs_get_counts(rtdbs_engine* engine, int32_t* nn, int on_device);
+
+/* The engine's device output buffers (label[W], cluster_id[W]); they hold
+ * the latest result until the next slide. */
+RTDBS_API int rtdbs_device_outputs(rtdbs_engine* engine, int32_t** d_label, int32_t** d_cluster_id);
+
+RTDBS_API int rtdbs_get_stats(rtdbs_engine* engine, rtdbs_stats* stats);
+
+/* rtdbs_slide_async with every kernel launched directly and bracketed by CUDA
+ * events; synchronous.  Results are identical to an ordinary slide. */
+RTDBS_API int rtdbs_slide_profiled(rtdbs_engine* engine, const float* d_new_points,
+                                   rtdbs_phase_times* times);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RTDBS_H */

@@ -1,0 +1,594 @@
+// rtdbs_engine.cpp -- host side of the C ABI declared in include/rtdbs.h.
+//
+// The engine replaces the reference's ScanState + dbscan() slide loop
+// (src/dbscan/state.h:23-129, src/dbscan/dbscan.cpp:2258-2364): all device
+// buffers are allocated once at creation (initialize_params,
+// src/dbscan/dbscan.cpp:30-132), every per-slide size stays on the device
+// (the reference reads three counts back per slide,
+// src/dbscan/dbscan.cpp:549,561-562), and a slide is one CUDA-graph replay.
+#include "rtdbs.h"
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "rtdbs_internal.h"
+
+using rtdbs::Ctl;
+using rtdbs::View;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return status;
+}
+
+#define CUDA_TRY(expr)                                                                  \
+    do {                                                                                \
+        cudaError_t _e = (expr);                                                        \
+        if (_e != cudaSuccess)                                                          \
+            return fail(_e == cudaErrorMemoryAllocation ? RTDBS_ERR_OOM : RTDBS_ERR_CUDA, \
+                        "%s failed: %s", #expr, cudaGetErrorString(_e));                \
+    } while (0)
+
+// Restores the caller's current device on scope exit.
+struct DeviceGuard {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceGuard(int dev) {
+        err = cudaGetDevice(&prev);
+        if (err == cudaSuccess && prev != dev) err = cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+std::mutex g_cfg_mutex;
+std::vector<char> g_configured;
+
+cudaError_t configure_device(int dev) {
+    std::lock_guard<std::mutex> lock(g_cfg_mutex);
+    if ((int)g_configured.size() <= dev) g_configured.resize(dev + 1, 0);
+    if (g_configured[dev]) return cudaSuccess;
+    cudaError_t e = rtdbs::configure_kernels();
+    if (e == cudaSuccess) g_configured[dev] = 1;
+    return e;
+}
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+struct rtdbs_engine {
+    rtdbs_params p{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    View v{};
+    int chunk = 0;           // C
+    int staging_points = 0;  // capacity of the staging buffer in points
+    void* dev_block = nullptr;
+    size_t dev_bytes = 0;
+    Ctl* h_ctl = nullptr;    // pinned mirror of the control block
+    bool geometry_ready = false;
+    bool loaded = false;
+    cudaGraphExec_t slide_graph = nullptr;
+    double cell_side = 0.0;
+};
+
+namespace {
+
+// Grid geometry: cell side L = Eps (1 + 2^-12) >= Eps (the margin covers the
+// rounding of both predicates and of the double cell coordinate), clamped
+// extents over the bounding box, L doubled until the key fits 50 bits.
+int set_geometry(rtdbs_engine* e, const float* bmin, const float* bmax, bool widen) {
+    const int dim = e->p.dim;
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    double L = e->p.eps * (1.0 + 1.0 / 4096.0);
+    for (int a = 0; a < dim; ++a) {
+        lo[a] = bmin[a];
+        hi[a] = bmax[a];
+        if (!(lo[a] <= hi[a]) || !std::isfinite(lo[a]) || !std::isfinite(hi[a]))
+            return fail(RTDBS_ERR_INVALID, "bounding box of axis %d is empty or not finite", a);
+        if (widen) {
+            const double m = std::max(0.25 * (hi[a] - lo[a]), 4.0 * L);
+            lo[a] -= m;
+            hi[a] += m;
+        }
+    }
+    long long ext[3] = {1, 1, 1};
+    for (int guard = 0; guard < 4096; ++guard) {
+        double prod = 1.0;
+        for (int a = 0; a < dim; ++a) {
+            const double n = std::floor((hi[a] - lo[a]) / L) + 1.0;
+            ext[a] = (long long)n;
+            prod *= n;
+        }
+        if (prod <= std::ldexp(1.0, rtdbs::kKeyBitsMax) - 1.0) break;
+        L *= 2.0;
+    }
+    unsigned long long prod = 1;
+    for (int a = 0; a < 3; ++a) prod *= (unsigned long long)ext[a];
+    int bits = 0;
+    while (bits < 64 && (1ull << bits) < prod) ++bits;
+    View& v = e->v;
+    for (int a = 0; a < 3; ++a) {
+        v.origin[a] = lo[a];
+        v.ext[a] = ext[a];
+    }
+    v.inv_cell = 1.0 / L;
+    v.key_bits = bits;
+    v.sort_passes = (bits + 7) / 8;
+    e->cell_side = L;
+    e->geometry_ready = true;
+    return RTDBS_OK;
+}
+
+// FP32 filter band of the FP64 predicate: [E(1 - 2^-20), E(1 + 2^-20)] rounded
+// outward to float.  The float evaluation of three rounded squares of rounded
+// differences has relative error <= gamma_5 ~ 3.0e-7 (Higham, Accuracy and
+// Stability of Numerical Algorithms, 2nd ed., Lemma 3.1); outside the band the
+// float value decides exactly as the double one would.
+void set_band(View& v, double eps) {
+    const double E = eps * eps;
+    const double m = 1.0 / 1048576.0;
+    const double lo = E * (1.0 - m), hi = E * (1.0 + m);
+    float flo = (float)lo, fhi = (float)hi;
+    if ((double)flo > lo) flo = std::nextafter(flo, 0.0f);
+    if ((double)fhi < hi) fhi = std::nextafter(fhi, INFINITY);
+    v.lo = flo;
+    v.hi = fhi;
+    v.E = E;
+    v.filter_ok = (E >= std::ldexp(1.0, -100) && E <= std::ldexp(1.0, 100)) ? 1 : 0;
+    const float r = (float)eps;
+    v.r2f = r * r;
+}
+
+int allocate(rtdbs_engine* e) {
+    const int W = e->p.window, S = e->p.stride, dim = e->p.dim;
+    View& v = e->v;
+    e->chunk = std::min(S, rtdbs::kChunkMax);
+    const int load_chunk = std::min(W, rtdbs::kChunkMax);
+    const int C = std::max(e->chunk, load_chunk);
+    e->staging_points = std::max(S, load_chunk);
+    unsigned long long P = 1024;
+    int pbits = 10;
+    while (P < 2ull * (unsigned long long)W) {
+        P <<= 1;
+        ++pbits;
+    }
+    v.pbits = pbits;
+    v.pmask = (unsigned)(P - 1);
+    v.max_items = W + W / 32 + 64;
+
+    struct Part {
+        void** ptr;
+        size_t bytes;
+    };
+    std::vector<Part> parts = {
+        {(void**)&v.ring, sizeof(float4) * W},
+        {(void**)&v.kslot, sizeof(unsigned long long) * W},
+        {(void**)&v.skey[0], sizeof(unsigned long long) * W},
+        {(void**)&v.skey[1], sizeof(unsigned long long) * W},
+        {(void**)&v.spt[0], sizeof(float4) * W},
+        {(void**)&v.spt[1], sizeof(float4) * W},
+        {(void**)&v.scnt[0], sizeof(int) * W},
+        {(void**)&v.scnt[1], sizeof(int) * W},
+        {(void**)&v.table[0], sizeof(ulonglong2) * P},
+        {(void**)&v.table[1], sizeof(ulonglong2) * P},
+        {(void**)&v.items, sizeof(int2) * v.max_items},
+        {(void**)&v.parent, sizeof(int) * W},
+        {(void**)&v.label, sizeof(int) * W},
+        {(void**)&v.cid, sizeof(int) * W},
+        {(void**)&v.nsort, sizeof(unsigned long long) * C},
+        {(void**)&v.xsort, sizeof(unsigned long long) * C},
+        {(void**)&v.nword, sizeof(unsigned long long) * C},
+        {(void**)&v.xword, sizeof(unsigned long long) * C},
+        {(void**)&v.xpt, sizeof(float4) * C},
+        {(void**)&v.staging, sizeof(float) * (size_t)e->staging_points * dim},
+        {(void**)&v.ctl, sizeof(Ctl)},
+    };
+    size_t total = 0;
+    for (auto& q : parts) total += align_up(q.bytes, 256);
+    CUDA_TRY(cudaMalloc(&e->dev_block, total));
+    e->dev_bytes = total;
+    char* base = static_cast<char*>(e->dev_block);
+    for (auto& q : parts) {
+        *q.ptr = base;
+        base += align_up(q.bytes, 256);
+    }
+    CUDA_TRY(cudaMemsetAsync(v.table[0], 0, sizeof(ulonglong2) * P, e->stream));
+    CUDA_TRY(cudaMemsetAsync(v.table[1], 0, sizeof(ulonglong2) * P, e->stream));
+    CUDA_TRY(cudaMemsetAsync(v.ctl, 0, sizeof(Ctl), e->stream));
+    CUDA_TRY(cudaMallocHost((void**)&e->h_ctl, sizeof(Ctl)));
+    std::memset(e->h_ctl, 0, sizeof(Ctl));
+    return RTDBS_OK;
+}
+
+int check_device_error(rtdbs_engine* e) {
+    if (e->h_ctl->err)
+        return fail(RTDBS_ERR_DEVICE, "device error bits 0x%x (1 table full, 2 union-find bound, "
+                    "4 work list full, 8 chunk bookkeeping)", e->h_ctl->err);
+    return RTDBS_OK;
+}
+
+int enqueue_slide(rtdbs_engine* e) {
+    const int S = e->p.stride, C = e->chunk;
+    const int nchunks = (S + C - 1) / C;
+    for (int j = 0; j < nchunks; ++j) {
+        const int c = std::min(C, S - j * C);
+        CUDA_TRY(rtdbs::launch_chunk_step(e->v, e->p.precision, j, c, 0, j * C, e->stream));
+    }
+    CUDA_TRY(rtdbs::launch_cluster(e->v, e->p.precision, 1, e->stream));
+    return RTDBS_OK;
+}
+
+// Enqueues one slide whose new points are already in the staging buffer.
+int run_slide(rtdbs_engine* e) {
+    if (e->p.flags & RTDBS_FLAG_NO_GRAPH) return enqueue_slide(e);
+    if (!e->slide_graph) {
+        cudaGraph_t g = nullptr;
+        CUDA_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_slide(e);
+        cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+        if (rc != RTDBS_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        CUDA_TRY(ce);
+        cudaError_t ie = cudaGraphInstantiate(&e->slide_graph, g, 0);
+        cudaGraphDestroy(g);
+        CUDA_TRY(ie);
+    }
+    CUDA_TRY(cudaGraphLaunch(e->slide_graph, e->stream));
+    return RTDBS_OK;
+}
+
+int copy_in(rtdbs_engine* e, const float* src, size_t npts, int on_device) {
+    const size_t bytes = sizeof(float) * npts * e->p.dim;
+    CUDA_TRY(cudaMemcpyAsync((void*)e->v.staging, src, bytes,
+                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                             e->stream));
+    return RTDBS_OK;
+}
+
+int copy_out(rtdbs_engine* e, int32_t* label, int32_t* cid, int on_device) {
+    const size_t bytes = sizeof(int) * e->p.window;
+    const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (label) CUDA_TRY(cudaMemcpyAsync(label, e->v.label, bytes, k, e->stream));
+    if (cid) CUDA_TRY(cudaMemcpyAsync(cid, e->v.cid, bytes, k, e->stream));
+    return RTDBS_OK;
+}
+
+int fetch_ctl_and_sync(rtdbs_engine* e) {
+    CUDA_TRY(cudaMemcpyAsync(e->h_ctl, e->v.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    return check_device_error(e);
+}
+
+}  // namespace
+
+extern "C" {
+
+int rtdbs_abi_version(void) { return RTDBS_ABI_VERSION; }
+
+const char* rtdbs_status_string(int status) {
+    switch (status) {
+        case RTDBS_OK: return "ok";
+        case RTDBS_ERR_INVALID: return "invalid argument";
+        case RTDBS_ERR_CUDA: return "CUDA runtime error";
+        case RTDBS_ERR_OOM: return "out of memory";
+        case RTDBS_ERR_STATE: return "call out of order";
+        case RTDBS_ERR_DEVICE: return "device-side bound hit";
+        case RTDBS_ERR_NO_DEVICE: return "no CUDA device";
+        default: return "unknown status";
+    }
+}
+
+const char* rtdbs_last_error(void) { return g_last_error.c_str(); }
+
+int rtdbs_params_init(rtdbs_params* params) {
+    if (!params) return fail(RTDBS_ERR_INVALID, "params is NULL");
+    std::memset(params, 0, sizeof(*params));
+    params->dim = 3;
+    params->window = 0;
+    params->stride = 0;
+    params->min_pts = 5;
+    params->eps = 0.0;
+    params->precision = RTDBS_PREC_FP64;
+    return RTDBS_OK;
+}
+
+int rtdbs_create(const rtdbs_params* params, void* cuda_stream, rtdbs_engine** out) {
+    if (!params || !out) return fail(RTDBS_ERR_INVALID, "params/out is NULL");
+    *out = nullptr;
+    const rtdbs_params& p = *params;
+    if (p.dim < 1 || p.dim > 3) return fail(RTDBS_ERR_INVALID, "dim must be 1..3 (got %d)", p.dim);
+    if (p.window <= 0 || p.stride <= 0 || p.stride > p.window)
+        return fail(RTDBS_ERR_INVALID, "need 0 < stride <= window (got W=%d S=%d)", p.window, p.stride);
+    if (p.window % p.stride != 0)
+        return fail(RTDBS_ERR_INVALID, "window %% stride must be 0 (got W=%d S=%d)", p.window, p.stride);
+    if (p.window > (1 << 30)) return fail(RTDBS_ERR_INVALID, "window too large");
+    if (!(p.eps > 0.0) || !std::isfinite(p.eps)) return fail(RTDBS_ERR_INVALID, "eps must be finite and > 0");
+    if (p.precision != RTDBS_PREC_FP64 && p.precision != RTDBS_PREC_FP32)
+        return fail(RTDBS_ERR_INVALID, "unknown precision mode %d", p.precision);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(RTDBS_ERR_NO_DEVICE, "no CUDA device available");
+    if (p.device < 0 || p.device >= ndev) return fail(RTDBS_ERR_INVALID, "device %d out of range", p.device);
+
+    DeviceGuard guard(p.device);
+    CUDA_TRY(guard.err);
+    CUDA_TRY(configure_device(p.device));
+    rtdbs_engine* e = new (std::nothrow) rtdbs_engine();
+    if (!e) return fail(RTDBS_ERR_OOM, "host allocation failed");
+    e->p = p;
+    e->device = p.device;
+    if (cuda_stream) {
+        e->stream = static_cast<cudaStream_t>(cuda_stream);
+    } else {
+        cudaError_t ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+        if (ce != cudaSuccess) {
+            delete e;
+            return fail(RTDBS_ERR_CUDA, "cudaStreamCreate failed: %s", cudaGetErrorString(ce));
+        }
+        e->own_stream = true;
+    }
+    View& v = e->v;
+    v.dim = p.dim;
+    v.W = p.window;
+    v.S = p.stride;
+    v.min_pts = p.min_pts;
+    v.units = p.window / p.stride;
+    set_band(v, p.eps);
+    int rc = allocate(e);
+    if (rc == RTDBS_OK) {
+        v.chunk = e->chunk;
+        if (p.has_bbox) rc = set_geometry(e, p.bbox_min, p.bbox_max, false);
+    }
+    if (rc != RTDBS_OK) {
+        rtdbs_destroy(e);
+        return rc;
+    }
+    *out = e;
+    return RTDBS_OK;
+}
+
+int rtdbs_destroy(rtdbs_engine* e) {
+    if (!e) return RTDBS_OK;
+    DeviceGuard guard(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->slide_graph) cudaGraphExecDestroy(e->slide_graph);
+    if (e->dev_block) cudaFree(e->dev_block);
+    if (e->h_ctl) cudaFreeHost(e->h_ctl);
+    if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return RTDBS_OK;
+}
+
+int rtdbs_load_window(rtdbs_engine* e, const float* points, int points_on_device) {
+    if (!e || !points) return fail(RTDBS_ERR_INVALID, "engine/points is NULL");
+    DeviceGuard guard(e->device);
+    CUDA_TRY(guard.err);
+    const int W = e->p.window, dim = e->p.dim;
+    if (!e->p.has_bbox) {
+        std::vector<float> host;
+        const float* h = points;
+        if (points_on_device) {
+            host.resize((size_t)W * dim);
+            CUDA_TRY(cudaMemcpy(host.data(), points, sizeof(float) * host.size(), cudaMemcpyDeviceToHost));
+            h = host.data();
+        }
+        float mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
+        for (int a = 0; a < dim; ++a) {
+            float lo = INFINITY, hi = -INFINITY;
+            for (int i = 0; i < W; ++i) {
+                const float x = h[(size_t)i * dim + a];
+                if (std::isfinite(x)) {
+                    lo = std::min(lo, x);
+                    hi = std::max(hi, x);
+                }
+            }
+            if (!(lo <= hi)) lo = hi = 0.0f;
+            mn[a] = lo;
+            mx[a] = hi;
+        }
+        int rc = set_geometry(e, mn, mx, true);
+        if (rc != RTDBS_OK) return rc;
+    }
+    // Restart from an empty window.
+    if (e->slide_graph) {
+        cudaGraphExecDestroy(e->slide_graph);
+        e->slide_graph = nullptr;
+    }
+    CUDA_TRY(cudaMemsetAsync(e->v.ctl, 0, sizeof(Ctl), e->stream));
+    CUDA_TRY(cudaMemsetAsync(e->v.table[0], 0, sizeof(ulonglong2) * ((size_t)e->v.pmask + 1), e->stream));
+    CUDA_TRY(cudaMemsetAsync(e->v.table[1], 0, sizeof(ulonglong2) * ((size_t)e->v.pmask + 1), e->stream));
+    const int C = std::min(W, rtdbs::kChunkMax);
+    View v = e->v;
+    v.chunk = C;  // load chunks tile the slots [0, W)
+    for (int j = 0, off = 0; off < W; ++j, off += C) {
+        const int c = std::min(C, W - off);
+        int rc = copy_in(e, points + (size_t)off * dim, c, points_on_device);
+        if (rc != RTDBS_OK) return rc;
+        CUDA_TRY(rtdbs::launch_chunk_step(v, e->p.precision, j, c, 1, 0, e->stream));
+    }
+    int rc = fetch_ctl_and_sync(e);
+    if (rc != RTDBS_OK) return rc;
+    e->loaded = true;
+    return RTDBS_OK;
+}
+
+int rtdbs_slide(rtdbs_engine* e, const float* new_points, int32_t* label, int32_t* cluster_id) {
+    if (!e || !new_points) return fail(RTDBS_ERR_INVALID, "engine/new_points is NULL");
+    if (!e->loaded) return fail(RTDBS_ERR_STATE, "rtdbs_load_window must come first");
+    DeviceGuard guard(e->device);
+    CUDA_TRY(guard.err);
+    int rc = copy_in(e, new_points, e->p.stride, 0);
+    if (rc == RTDBS_OK) rc = run_slide(e);
+    if (rc == RTDBS_OK) rc = copy_out(e, label, cluster_id, 0);
+    if (rc == RTDBS_OK) rc = fetch_ctl_and_sync(e);
+    return rc;
+}
+
+int rtdbs_slide_async(rtdbs_engine* e, const float* d_new_points, int32_t* d_label,
+                      int32_t* d_cluster_id) {
+    if (!e || !d_new_points) return fail(RTDBS_ERR_INVALID, "engine/new_points is NULL");
+    if (!e->loaded) return fail(RTDBS_ERR_STATE, "rtdbs_load_window must come first");
+    DeviceGuard guard(e->device);
+    CUDA_TRY(guard.err);
+    int rc = RTDBS_OK;
+    if (d_new_points != e->v.staging) rc = copy_in(e, d_new_points, e->p.stride, 1);
+    if (rc == RTDBS_OK) rc = run_slide(e);
+    if (rc == RTDBS_OK && (d_label || d_cluster_id)) rc = copy_out(e, d_label, d_cluster_id, 1);
+    return rc;
+}
+
+int rtdbs_sync(rtdbs_engine* e) {
+    if (!e) return fail(RTDBS_ERR_INVALID, "engine is NULL");
+    DeviceGuard guard(e->device);
+    CUDA_TRY(guard.err);
+    return fetch_ctl_and_sync(e);
+}
+
+int rtdbs_cluster(rtdbs_engine* e, int32_t* label, int32_t* cluster_id, int on_device) {
+    if (!e) return fail(RTDBS_ERR_INVALID, "engine is NULL");
+    if (!e->loaded) return fail(RTDBS_ERR_STATE, "rtdbs_load_window must come first");
+    DeviceGuard guard(e->device);
+    CUDA_TRY(guard.err);
+    CUDA_TRY(rtdbs::launch_cluster(e->v, e->p.precision, 0, e->stream));
+    int rc = copy_out(e, label, cluster_id, on_device);
+    if (rc == RTDBS_OK) rc = fetch_ctl_and_sync(e);
+    return rc;
+}
+
+int rtdbs_get_counts(rtdbs_engine* e, int32_t* nn, int on_device) {
+    if (!e || !nn) return fail(RTDBS_ERR_INVALID, "engine/nn is NULL");
+    if (!e->loaded) return fail(RTDBS_ERR_STATE, "rtdbs_load_window must come first");
+    DeviceGuard guard(e->device);
+    CUDA_TRY(guard.err);
+    if (on_device) {
+        CUDA_TRY(rtdbs::launch_counts_by_slot(e->v, nn, e->stream));
+    } else {
+        // the label buffer is free scratch between slides only if we restore it;
+        // use a temporary device buffer instead
+        int* tmp = nullptr;
+        CUDA_TRY(cudaMallocAsync((void**)&tmp, sizeof(int) * e->p.window, e->stream));
+        cudaError_t ce = rtdbs::launch_counts_by_slot(e->v, tmp, e->stream);
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(nn, tmp, sizeof(int) * e->p.window, cudaMemcpyDeviceToHost, e->stream);
+        cudaFreeAsync(tmp, e->stream);
+        CUDA_TRY(ce);
+    }
+    return fetch_ctl_and_sync(e);
+}
+
+int rtdbs_device_outputs(rtdbs_engine* e, int32_t** d_label, int32_t** d_cluster_id) {
+    if (!e) return fail(RTDBS_ERR_INVALID, "engine is NULL");
+    if (d_label) *d_label = e->v.label;
+    if (d_cluster_id) *d_cluster_id = e->v.cid;
+    return RTDBS_OK;
+}
+
+int rtdbs_get_stats(rtdbs_engine* e, rtdbs_stats* s) {
+    if (!e || !s) return fail(RTDBS_ERR_INVALID, "engine/stats is NULL");
+    DeviceGuard guard(e->device);
+    CUDA_TRY(guard.err);
+    CUDA_TRY(cudaMemcpyAsync(e->h_ctl, e->v.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    std::memset(s, 0, sizeof(*s));
+    s->slides = e->h_ctl->slide;
+    s->band_rechecks = (int64_t)e->h_ctl->band_rechecks;
+    s->cells = e->h_ctl->ncells;
+    s->work_items = e->h_ctl->nitems;
+    s->error_bits = e->h_ctl->err;
+    s->key_bits = e->v.key_bits;
+    s->cell_side = e->cell_side;
+    s->device_bytes = (int64_t)e->dev_bytes;
+    const int nchunks = (e->p.stride + e->chunk - 1) / e->chunk;
+    s->chunks_per_slide = nchunks;
+    s->launches_per_slide = nchunks * rtdbs::kChunkPhases + 2;
+    return RTDBS_OK;
+}
+
+int rtdbs_slide_profiled(rtdbs_engine* e, const float* d_new_points, rtdbs_phase_times* t) {
+    if (!e || !d_new_points || !t) return fail(RTDBS_ERR_INVALID, "engine/new_points/times is NULL");
+    if (!e->loaded) return fail(RTDBS_ERR_STATE, "rtdbs_load_window must come first");
+    DeviceGuard guard(e->device);
+    CUDA_TRY(guard.err);
+    const int S = e->p.stride, C = e->chunk;
+    const int nchunks = (S + C - 1) / C;
+    const int nev = nchunks * rtdbs::kChunkPhases + 3;
+    std::vector<cudaEvent_t> ev(nev, nullptr);
+    for (auto& x : ev) CUDA_TRY(cudaEventCreate(&x));
+    int rc = RTDBS_OK;
+    if (d_new_points != e->v.staging) rc = copy_in(e, d_new_points, S, 1);
+    int k = 0;
+    if (rc == RTDBS_OK) {
+        cudaEventRecord(ev[k++], e->stream);
+        for (int j = 0; j < nchunks && rc == RTDBS_OK; ++j) {
+            const int c = std::min(C, S - j * C);
+            for (int ph = 0; ph < rtdbs::kChunkPhases; ++ph) {
+                cudaError_t ce = rtdbs::launch_phase(ph, e->v, e->p.precision, j, c, 0, j * C, 0, e->stream);
+                if (ce != cudaSuccess) {
+                    rc = fail(RTDBS_ERR_CUDA, "launch failed: %s", cudaGetErrorString(ce));
+                    break;
+                }
+                cudaEventRecord(ev[k++], e->stream);
+            }
+        }
+        for (int ph = rtdbs::kPhaseUnion; ph <= rtdbs::kPhaseLabel && rc == RTDBS_OK; ++ph) {
+            cudaError_t ce = rtdbs::launch_phase(ph, e->v, e->p.precision, 0, 0, 0, 0, 1, e->stream);
+            if (ce != cudaSuccess) rc = fail(RTDBS_ERR_CUDA, "launch failed: %s", cudaGetErrorString(ce));
+            cudaEventRecord(ev[k++], e->stream);
+        }
+    }
+    if (rc == RTDBS_OK) rc = fetch_ctl_and_sync(e);
+    if (rc == RTDBS_OK) {
+        float ph[rtdbs::kNumPhases] = {0};
+        int q = 0;
+        for (int j = 0; j < nchunks; ++j)
+            for (int p = 0; p < rtdbs::kChunkPhases; ++p, ++q) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, ev[q], ev[q + 1]);
+                ph[p] += ms;
+            }
+        for (int p = rtdbs::kPhaseUnion; p <= rtdbs::kPhaseLabel; ++p, ++q) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[q], ev[q + 1]);
+            ph[p] += ms;
+        }
+        float total = 0.f;
+        cudaEventElapsedTime(&total, ev[0], ev[q]);
+        t->ingest_ms = ph[rtdbs::kPhaseIngest];
+        t->sort_ms = ph[rtdbs::kPhaseSort];
+        t->decrement_ms = ph[rtdbs::kPhaseDecrement];
+        t->merge_ms = ph[rtdbs::kPhaseMerge];
+        t->build_ms = ph[rtdbs::kPhaseBuild];
+        t->increment_ms = ph[rtdbs::kPhaseIncrement];
+        t->union_ms = ph[rtdbs::kPhaseUnion];
+        t->label_ms = ph[rtdbs::kPhaseLabel];
+        t->total_ms = total;
+        t->chunks = nchunks;
+    }
+    for (auto& x : ev)
+        if (x) cudaEventDestroy(x);
+    return rc;
+}
+
+}  // extern "C"

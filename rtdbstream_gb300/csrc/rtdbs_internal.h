@@ -1,0 +1,122 @@
+// rtdbs_internal.h -- device-side state layout shared by the kernels and the
+// host engine of the streaming DBSCAN path.
+//
+// HBM layout of one stream (W slots, chunk C <= kChunkMax points):
+//   ring   float4[W]      point of each ring slot (x, y, z, slot bits); the
+//                         reference's params.window (src/dbscan/dbscan.h:23)
+//   kslot  u64[W]         cell key of each slot (reference: point_cell_id)
+//   skey   u64[2][W]      window sorted by (cell key, slot): keys
+//   spt    float4[2][W]   ... points in that order (.w = slot as int bits)
+//   scnt   i32[2][W]      ... exact neighbour count in that order
+//                         (double-buffered; the reference's pos_arr/
+//                         tmp_pos_arr, src/dbscan/grid.cpp:181-199)
+//   table  {u64,u64}[2][P] open-addressed cell table: tagged key -> [start,end)
+//                         (replaces the OptiX BVH, src/dbscan/optix.cpp:438-483)
+//   items  int2[W+W/32+64] work list: runs of <= 32 sorted points of one cell
+//   parent i32[W]         union-find forest by slot (reference: cluster_id)
+//   label, cid i32[W]     outputs by slot
+//   chunk scratch: sort words, expired points.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rtdbs {
+
+constexpr int kChunkMax = 16384;   // points per grid-update chunk (one-CTA radix sort)
+constexpr int kOffBits = 14;       // in-chunk offset bits of a sort word
+constexpr int kKeyBitsMax = 50;    // cell-key bits (key << 14 | offset fits in 64 bits)
+constexpr unsigned long long kKeyMask = (1ull << kKeyBitsMax) - 1ull;
+constexpr unsigned kGenMod = 16383;  // table generations 1..16383 (tag = gen << 50 | key)
+constexpr int kMergeTile = 1024;   // old entries per merge block
+constexpr int kMergeThreads = 256;
+constexpr int kSortThreads = 1024;
+constexpr int kMaxIter = 1 << 20;  // bound on every device-side retry loop
+
+// Bits of Ctl::err.
+constexpr int kErrHashFull = 1;
+constexpr int kErrUnionIter = 2;
+constexpr int kErrItems = 4;
+constexpr int kErrChunk = 8;
+
+// Device-resident control block of one stream.  Every field that changes
+// from slide to slide lives here (not in kernel arguments), so one captured
+// CUDA graph replays every slide.
+struct Ctl {
+    long long b;               // grid builds so far (merge + table build)
+    long long slide;           // slides completed
+    int nocc[2];               // entries in sorted buffer 0 / 1
+    int nitems;                // work items of the current grid
+    int ncells;                // cells of the current grid
+    int err;                   // kErr* bits
+    int pad0;
+    unsigned long long band_rechecks;
+    long long reserved[4];
+};
+
+// Everything a kernel needs for one stream, passed by value.
+struct View {
+    // geometry: cell (i, j, k) = clamp(floor((x - origin) * inv_cell)),
+    // key = (i * ext[1] + j) * ext[2] + k
+    double origin[3];
+    double inv_cell;
+    long long ext[3];
+    int dim;
+    // parameters
+    int W, S, min_pts, units;   // units = W / S
+    int chunk;                  // C
+    int pbits;                  // log2 of table capacity
+    unsigned pmask;
+    float r2f;                  // FP32 mode: (float)eps * (float)eps
+    float lo, hi;               // FP64 mode: FP32 filter band
+    double E;                   // FP64 mode: eps * eps
+    int filter_ok;              // FP64 mode: band valid (else every test in FP64)
+    int key_bits;
+    int sort_passes;
+    int max_items;
+    // buffers
+    float4* ring;
+    unsigned long long* kslot;
+    unsigned long long* skey[2];
+    float4* spt[2];
+    int* scnt[2];
+    ulonglong2* table[2];
+    int2* items;
+    int* parent;
+    int* label;
+    int* cid;
+    unsigned long long* nsort;   // chunk sort words in (key << 14 | offset)
+    unsigned long long* xsort;
+    unsigned long long* nword;   // sorted
+    unsigned long long* xword;
+    float4* xpt;                 // expired points of the chunk by offset
+    const float* staging;        // new points [S][dim]
+    Ctl* ctl;
+};
+
+// Kernel phases of a slide, in launch order.
+enum Phase : int {
+    kPhaseIngest = 0,
+    kPhaseSort,
+    kPhaseDecrement,
+    kPhaseMerge,
+    kPhaseBuild,
+    kPhaseIncrement,
+    kPhaseUnion,
+    kPhaseLabel,
+    kNumPhases
+};
+constexpr int kChunkPhases = 6;  // ingest .. increment, once per chunk
+
+// Launchers (rtdbs_kernels.cu).  j = chunk index within the slide (or the
+// load), c = points in the chunk, init = 1 while loading the first window,
+// advance = 1 when the label phase ends a slide.
+cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, int init,
+                         int staging_offset, int advance, cudaStream_t s);
+cudaError_t launch_chunk_step(const View& v, int precision, int j, int c, int init,
+                              int staging_offset, cudaStream_t s);
+cudaError_t launch_cluster(const View& v, int precision, int advance, cudaStream_t s);
+cudaError_t launch_counts_by_slot(const View& v, int* nn_by_slot, cudaStream_t s);
+cudaError_t configure_kernels();
+
+}  // namespace rtdbs

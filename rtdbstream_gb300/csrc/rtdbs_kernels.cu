@@ -1,0 +1,938 @@
+// rtdbs_kernels.cu -- sm_103a kernels of the per-slide streaming DBSCAN path.
+//
+// One slide = ceil(S / C) grid-update chunk steps followed by one clustering
+// step (reference level-9 loop, src/dbscan/dbscan.cpp:2276-2362):
+//
+//   chunk step (C <= 16384 new points replacing the points of the same slots)
+//     k_ingest  new points -> ring slots + cell keys; expired points saved
+//               (reference: H2D 2289 + compute_cell_id, src/dbscan/aabb.cu:589-610)
+//     k_sort    one-CTA LSD radix sort of the new and of the expired
+//               (cell key, slot) words (reference: sortByCellIdAndOrder,
+//               src/dbscan/thrust_helper.cu:21-29)
+//     k_decr    exact -1 on the neighbour counts of every survivor within Eps
+//               of an expired point, on the old grid
+//     k_merge   old sorted window minus expired plus new, one pass, merge-path
+//               tiles (reference: merge_by_cell_id_and_idx,
+//               src/dbscan/thrust_helper.cu:31-51)
+//     k_build   cell table (tagged open addressing) + work list of cell runs
+//               (replaces compute_offsets_of_cells / set_hybrid_spheres_info /
+//               optixAccelBuild, src/dbscan/aabb.cu:377-544,
+//               src/dbscan/optix.cpp:438-483)
+//     k_incr    full count of every new point and exact +1 on its neighbours
+//               on the new grid (reference: __raygen__grid/__intersection__grid,
+//               src/dbscan/dbscan.cu:155-194,250-270, which recounts all W)
+//   clustering step
+//     k_union   union-find over core-core pairs, each unordered pair once
+//               (reference: __raygen__cluster/__intersection__hybrid_radius_sphere,
+//               src/dbscan/dbscan.cu:279-321,354-394; find_repres/unite 9-43)
+//     k_label   labels and ids by slot; border = minimum id of the adjacent
+//               clusters (reference: set_label_kernel + post_cluster_t,
+//               src/dbscan/aabb.cu:173-196,575-587)
+//
+// Neighbour predicate: a warp holds 32 candidates in lanes (coalesced float4
+// loads of the cell-sorted window) and tests them against home points
+// broadcast by shuffle.  Squared distances use explicitly rounded IEEE
+// operations (no FMA contraction), so FP32 mode is bit-identical to the
+// reference's CPU checker (src/dbscan/util.cpp:308-316).
+#include "rtdbs_internal.h"
+
+#include <climits>
+#include <cstdint>
+
+namespace rtdbs {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kPrecFp64 = 0;
+constexpr int kPrecFp32 = 1;
+
+__device__ __forceinline__ int slot_of(const float4& p) { return __float_as_int(p.w); }
+
+__device__ __forceinline__ unsigned lanemask_lt(int lane) { return (1u << lane) - 1u; }
+
+// ------------------------------------------------------------------ geometry
+
+__device__ __forceinline__ unsigned long long cell_key(const View& v, float x, float y, float z) {
+    const float q[3] = {x, y, z};
+    unsigned long long key = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        long long c = 0;
+        if (a < v.dim) {
+            double t = floor(((double)q[a] - v.origin[a]) * v.inv_cell);
+            if (!(t >= 0.0)) t = 0.0;  // also maps NaN to cell 0
+            const double top = (double)(v.ext[a] - 1);
+            if (t > top) t = top;
+            c = (long long)t;
+        }
+        key = key * (unsigned long long)v.ext[a] + (unsigned long long)c;
+    }
+    return key;
+}
+
+__device__ __forceinline__ unsigned gen_of_build(long long b) {
+    return (unsigned)((b >> 1) % (long long)kGenMod) + 1u;
+}
+
+__device__ __forceinline__ int chunk_base_slot(const View& v, int j, int init) {
+    const int base = init ? 0 : (int)(v.ctl->slide % v.units) * v.S;
+    return base + j * v.chunk;
+}
+
+// ----------------------------------------------------------------- predicate
+
+template <int DIM>
+__device__ __forceinline__ float sqdist32(const float4& a, const float4& b) {
+    const float dx = __fsub_rn(a.x, b.x);
+    float d = __fmul_rn(dx, dx);
+    if (DIM > 1) {
+        const float dy = __fsub_rn(a.y, b.y);
+        d = __fadd_rn(d, __fmul_rn(dy, dy));
+    }
+    if (DIM > 2) {
+        const float dz = __fsub_rn(a.z, b.z);
+        d = __fadd_rn(d, __fmul_rn(dz, dz));
+    }
+    return d;
+}
+
+template <int DIM>
+__device__ __forceinline__ double sqdist64(const float4& a, const float4& b) {
+    const double dx = __dsub_rn((double)a.x, (double)b.x);
+    double d = __dmul_rn(dx, dx);
+    if (DIM > 1) {
+        const double dy = __dsub_rn((double)a.y, (double)b.y);
+        d = __dadd_rn(d, __dmul_rn(dy, dy));
+    }
+    if (DIM > 2) {
+        const double dz = __dsub_rn((double)a.z, (double)b.z);
+        d = __dadd_rn(d, __dmul_rn(dz, dz));
+    }
+    return d;
+}
+
+// Neighbour test of two distinct points.  FP32 mode: the reference predicate
+// d32 < r2f.  FP64 mode: d32 < lo and d32 >= hi are decided by the float
+// value (the band [lo, hi) around Eps^2 bounds the float evaluation's
+// rounding error, see oracle_band); everything else in double.
+template <int MODE, int DIM>
+__device__ __forceinline__ bool is_nbr(const View& v, const float4& a, const float4& b,
+                                       unsigned& rechecks) {
+    const float d = sqdist32<DIM>(a, b);
+    if (MODE == kPrecFp32) return d < v.r2f;
+    if (v.filter_ok) {
+        if (d < v.lo) return true;
+        if (d >= v.hi) return false;
+    }
+    ++rechecks;
+    return sqdist64<DIM>(a, b) < v.E;
+}
+
+// ---------------------------------------------------------------- cell table
+
+__device__ __forceinline__ unsigned table_home(unsigned long long key, int pbits) {
+    return (unsigned)((key * 0x9E3779B97F4A7C15ull) >> (64 - pbits));
+}
+
+__device__ __forceinline__ unsigned long long tag_of(unsigned long long key, unsigned gen) {
+    return ((unsigned long long)gen << kKeyBitsMax) | key;
+}
+
+// [start, end) of a cell, (0, 0) if the cell is empty in this generation.
+__device__ __forceinline__ int2 table_find(const ulonglong2* T, unsigned pmask, int pbits,
+                                           unsigned long long tag) {
+    unsigned s = table_home(tag & kKeyMask, pbits);
+    const unsigned long long gen = tag >> kKeyBitsMax;
+    for (unsigned i = 0; i <= pmask; ++i) {
+        const ulonglong2 e = T[s];
+        if (e.x == tag) return make_int2((int)(unsigned)e.y, (int)(unsigned)(e.y >> 32));
+        if ((e.x >> kKeyBitsMax) != gen) break;  // empty or stale slot ends the probe
+        s = (s + 1) & pmask;
+    }
+    return make_int2(0, 0);
+}
+
+// Claims (or finds) the slot of `tag` and stores one half of its range:
+// which = 0 -> start, 1 -> end.  Entries of older generations count as free.
+__device__ bool table_set(ulonglong2* T, unsigned pmask, int pbits, unsigned long long tag,
+                          int which, int value) {
+    unsigned s = table_home(tag & kKeyMask, pbits);
+    const unsigned long long gen = tag >> kKeyBitsMax;
+    for (unsigned i = 0; i <= pmask; ++i) {
+        unsigned long long* kp = reinterpret_cast<unsigned long long*>(&T[s].x);
+        unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(kp);
+        for (int t = 0; t < 8; ++t) {
+            if (cur == tag) {
+                reinterpret_cast<int*>(&T[s].y)[which] = value;
+                return true;
+            }
+            if ((cur >> kKeyBitsMax) == gen) break;  // another cell of this generation
+            const unsigned long long prev = atomicCAS(kp, cur, tag);
+            if (prev == cur) {
+                reinterpret_cast<int*>(&T[s].y)[which] = value;
+                return true;
+            }
+            cur = prev;
+        }
+        s = (s + 1) & pmask;
+    }
+    return false;
+}
+
+// Row ranges of the 3^DIM cells around `key`.  The three cells of a row
+// (last axis -1, 0, +1) have consecutive keys, so they occupy one contiguous
+// range of the cell-sorted window.  On return lane r < 3^(DIM-1) holds row r
+// as [rs, re) (empty rows: rs == re).
+template <int DIM>
+__device__ __forceinline__ void row_ranges(const View& v, const ulonglong2* T, unsigned gen,
+                                           unsigned long long key, int lane, int& rs, int& re) {
+    constexpr int kCells = DIM == 1 ? 3 : (DIM == 2 ? 9 : 27);
+    const long long e1 = v.ext[1], e2 = v.ext[2];
+    const long long c2 = (long long)(key % (unsigned long long)e2);
+    const long long rr = (long long)(key / (unsigned long long)e2);
+    const long long c1 = rr % e1;
+    const long long c0 = rr / e1;
+    int2 rg = make_int2(0, 0);
+    if (lane < kCells) {
+        long long q0 = c0, q1 = c1, q2 = c2;
+        if (DIM == 1) {
+            q0 += lane - 1;
+        } else if (DIM == 2) {
+            q0 += lane / 3 - 1;
+            q1 += lane % 3 - 1;
+        } else {
+            q0 += lane / 9 - 1;
+            q1 += (lane / 3) % 3 - 1;
+            q2 += lane % 3 - 1;
+        }
+        const bool ok = q0 >= 0 && q0 < v.ext[0] && q1 >= 0 && q1 < e1 && q2 >= 0 && q2 < e2;
+        if (ok) {
+            const unsigned long long nk =
+                ((unsigned long long)q0 * (unsigned long long)e1 + (unsigned long long)q1) *
+                    (unsigned long long)e2 + (unsigned long long)q2;
+            rg = table_find(T, v.pmask, v.pbits, tag_of(nk, gen));
+        }
+    }
+    int s = INT_MAX, e = INT_MIN;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int src = min(3 * lane + k, 31);
+        const int a = __shfl_sync(kFull, rg.x, src);
+        const int b = __shfl_sync(kFull, rg.y, src);
+        if (b > a) {
+            s = min(s, a);
+            e = max(e, b);
+        }
+    }
+    if (e == INT_MIN) s = e = 0;
+    rs = s;
+    re = e;
+}
+
+// ---------------------------------------------------------------- union-find
+
+// Root of v with intermediate pointer jumping (each visited node is pointed
+// at its grandparent).  Parents only ever decrease, so the walk terminates.
+__device__ __forceinline__ int uf_find(int* parent, int v) {
+    volatile int* P = parent;
+    int curr = P[v];
+    if (curr != v) {
+        int next, prev = v;
+        while (curr > (next = P[curr])) {
+            P[prev] = next;
+            prev = curr;
+            curr = next;
+        }
+    }
+    return curr;
+}
+
+// Lock-free union: the larger root is hooked under the smaller one with
+// atomicCAS, so every root is the minimum slot of its set.
+__device__ __forceinline__ void uf_unite(int* parent, int a, int b, int& err) {
+    int ra = uf_find(parent, a);
+    int rb = uf_find(parent, b);
+    for (int it = 0; it < kMaxIter; ++it) {
+        if (ra == rb) return;
+        if (ra < rb) {
+            const int t = ra;
+            ra = rb;
+            rb = t;
+        }
+        const int old = atomicCAS(&parent[ra], ra, rb);
+        if (old == ra) return;
+        ra = uf_find(parent, old);
+    }
+    err |= kErrUnionIter;
+}
+
+__device__ __forceinline__ void flush_stats(const View& v, unsigned rechecks, int err, int lane) {
+    unsigned r = rechecks;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(kFull, r, o);
+    const int e = __reduce_or_sync(kFull, (unsigned)err);
+    if (lane == 0) {
+        if (r) atomicAdd(&v.ctl->band_rechecks, (unsigned long long)r);
+        if (e) atomicOr(&v.ctl->err, e);
+    }
+}
+
+__device__ __forceinline__ float4 shfl_pt(const float4& p, int src) {
+    return make_float4(__shfl_sync(kFull, p.x, src), __shfl_sync(kFull, p.y, src),
+                       __shfl_sync(kFull, p.z, src), __shfl_sync(kFull, p.w, src));
+}
+
+// ------------------------------------------------------------------- kernels
+
+// New points of chunk j -> ring slots [el, el+c): float4 + cell key; the
+// points they replace are kept for the decrement pass.
+__global__ void k_ingest(View v, int j, int c, int init, int stg_off) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) v.ctl->b += 1;  // no reader in this kernel
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c) return;
+    const int slot = chunk_base_slot(v, j, init) + k;
+    if (!init) {
+        v.xpt[k] = v.ring[slot];
+        v.xsort[k] = (v.kslot[slot] << kOffBits) | (unsigned long long)k;
+    }
+    const float* p = v.staging + (size_t)(stg_off + k) * v.dim;
+    const float x = p[0];
+    const float y = v.dim > 1 ? p[1] : 0.0f;
+    const float z = v.dim > 2 ? p[2] : 0.0f;
+    v.ring[slot] = make_float4(x, y, z, __int_as_float(slot));
+    const unsigned long long key = cell_key(v, x, y, z);
+    v.kslot[slot] = key;
+    v.nsort[k] = (key << kOffBits) | (unsigned long long)k;
+}
+
+// Exclusive scan of one value per thread over a 1024-thread block.
+__device__ __forceinline__ unsigned block_excl_scan_1024(unsigned val, unsigned* wsum) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned incl = val;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        const unsigned x = wsum[lane];
+        unsigned xi = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned t = __shfl_up_sync(kFull, xi, o);
+            if (lane >= o) xi += t;
+        }
+        wsum[lane] = xi - x;
+    }
+    __syncthreads();
+    const unsigned r = wsum[w] + incl - val;
+    __syncthreads();
+    return r;
+}
+
+// One-CTA stable LSD radix sort (8-bit digits over the key bits of the sort
+// word) of c <= 16384 words; block 0 sorts the new words, block 1 the
+// expired ones.  Warp-level multisplit: lanes with equal digits are ranked by
+// __match_any_sync; per-(digit, warp) counters are scanned in digit-major
+// order so the order of equal digits is the item order.
+__global__ void __launch_bounds__(kSortThreads, 1) k_sort(View v, int c, int init) {
+    extern __shared__ unsigned long long sort_smem[];
+    __shared__ unsigned wsum[32];
+    unsigned long long* buf = sort_smem;                                       // kChunkMax words
+    unsigned* whist = reinterpret_cast<unsigned*>(sort_smem + kChunkMax);       // 256 x 32
+    const int which = blockIdx.x;
+    if (which == 1 && init) return;
+    const unsigned long long* in = which ? v.xsort : v.nsort;
+    unsigned long long* out = which ? v.xword : v.nword;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int ipt = (c + kSortThreads - 1) / kSortThreads;  // 1..16
+    const int wbase = w * 32 * ipt;
+    const unsigned lt = lanemask_lt(lane);
+    unsigned long long it[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+        const int idx = wbase + r * 32 + lane;
+        it[r] = (r < ipt && idx < c) ? in[idx] : ~0ull;
+    }
+    for (int pass = 0; pass < v.sort_passes; ++pass) {
+        const int shift = kOffBits + 8 * pass;
+        for (int i = tid; i < 256 * 32; i += kSortThreads) whist[i] = 0;
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            if (r < ipt) {
+                const unsigned d = (unsigned)(it[r] >> shift) & 255u;
+                const unsigned peers = __match_any_sync(kFull, d);
+                if ((peers & lt) == 0) whist[d * 32 + w] += __popc(peers);
+            }
+        }
+        __syncthreads();
+        unsigned loc[8];
+        unsigned sum = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            loc[k] = whist[tid * 8 + k];
+            sum += loc[k];
+        }
+        unsigned pre = block_excl_scan_1024(sum, wsum);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            whist[tid * 8 + k] = pre;
+            pre += loc[k];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            if (r < ipt) {
+                const unsigned d = (unsigned)(it[r] >> shift) & 255u;
+                const unsigned peers = __match_any_sync(kFull, d);
+                const unsigned base = whist[d * 32 + w];
+                __syncwarp();
+                if ((peers & lt) == 0) whist[d * 32 + w] = base + __popc(peers);
+                __syncwarp();
+                buf[base + __popc(peers & lt)] = it[r];
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < 16; ++r)
+            if (r < ipt) it[r] = buf[wbase + r * 32 + lane];
+        __syncthreads();
+    }
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+        const int idx = wbase + r * 32 + lane;
+        if (r < ipt && idx < c) out[idx] = it[r];
+    }
+}
+
+// -1 on the count of every surviving neighbour of each expired point (old grid).
+template <int MODE, int DIM>
+__global__ void k_decr(View v, int j, int c) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (gw >= c) return;
+    const long long b = v.ctl->b;
+    const int old = (int)((b - 1) & 1);
+    const unsigned gen = gen_of_build(b - 1);
+    const int el = chunk_base_slot(v, j, 0);
+    const unsigned long long word = v.xword[gw];
+    const unsigned long long key = word >> kOffBits;
+    const float4 xp = v.xpt[word & ((1u << kOffBits) - 1)];
+    int rs, re;
+    row_ranges<DIM>(v, v.table[old], gen, key, lane, rs, re);
+    const float4* spt = v.spt[old];
+    int* scnt = v.scnt[old];
+    unsigned rechecks = 0;
+    constexpr int kRows = DIM == 1 ? 1 : (DIM == 2 ? 3 : 9);
+#pragma unroll 1
+    for (int r = 0; r < kRows; ++r) {
+        const int a = __shfl_sync(kFull, rs, r), e = __shfl_sync(kFull, re, r);
+        for (int base = a; base < e; base += 32) {
+            const int pos = base + lane;
+            if (pos < e) {
+                const float4 q = spt[pos];
+                const int qs = slot_of(q);
+                if ((qs < el || qs >= el + c) && is_nbr<MODE, DIM>(v, xp, q, rechecks))
+                    atomicSub(&scnt[pos], 1);
+            }
+        }
+    }
+    flush_stats(v, rechecks, 0, lane);
+}
+
+__device__ __forceinline__ bool tuple_less(unsigned long long ka, int sa, unsigned long long kb,
+                                           int sb) {
+    return ka < kb || (ka == kb && sa < sb);
+}
+
+// Number of sorted chunk words (key, el + offset) strictly below (key, slot).
+__device__ __forceinline__ int count_words_less(const unsigned long long* words, int n, int el,
+                                                unsigned long long key, int slot) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const unsigned long long w = words[mid];
+        if (tuple_less(w >> kOffBits, el + (int)(w & ((1u << kOffBits) - 1)), key, slot))
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// Old sorted window minus the expired slots [el, el+c), merged with the c
+// new entries; tile t of the old window goes to output offset
+// ts - (#expired before ts) + (#new before old[ts]).
+__global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, int init) {
+    __shared__ unsigned long long tkey[kMergeTile];
+    __shared__ int tslot[kMergeTile];
+    __shared__ int spre[kMergeTile + 1];
+    __shared__ unsigned wsum[32];
+    const long long b = v.ctl->b;
+    const int src = (int)((b - 1) & 1), dst = (int)(b & 1);
+    const int n_old = v.ctl->nocc[src];
+    const int n_new = n_old - (init ? 0 : c) + c;
+    const int el = chunk_base_slot(v, j, init);
+    const int tid = threadIdx.x;
+    if (blockIdx.x == 0 && tid == 0) {
+        v.ctl->nocc[dst] = n_new;
+        v.ctl->nitems = 0;
+        v.ctl->ncells = 0;
+    }
+    // Table generations wrap every kGenMod builds of a table: clear it then.
+    if (b >= 2 && ((b >> 1) % (long long)kGenMod) == 0) {
+        ulonglong2* T = v.table[dst];
+        for (unsigned i = blockIdx.x * blockDim.x + tid; i <= v.pmask; i += gridDim.x * blockDim.x)
+            T[i] = make_ulonglong2(0ull, 0ull);
+    }
+    const int ntiles = n_old > 0 ? (n_old + kMergeTile - 1) / kMergeTile : 1;
+    const int t = blockIdx.x;
+    if (t >= ntiles) return;
+    const int ts = t * kMergeTile;
+    const int te = min(ts + kMergeTile, n_old);
+    const int tlen = te - ts;
+    const unsigned long long* okey = v.skey[src];
+    const float4* opt = v.spt[src];
+    const int* ocnt = v.scnt[src];
+    unsigned long long* dkey = v.skey[dst];
+    float4* dpt = v.spt[dst];
+    int* dcnt = v.scnt[dst];
+
+    int jt0 = 0, jt1 = c, e0 = 0;
+    if (tlen > 0) {
+        const unsigned long long k0 = okey[ts];
+        const int s0 = slot_of(opt[ts]);
+        if (t > 0) jt0 = count_words_less(v.nword, c, el, k0, s0);
+        if (!init) e0 = count_words_less(v.xword, c, el, k0, s0);
+        if (t < ntiles - 1) jt1 = count_words_less(v.nword, c, el, okey[te], slot_of(opt[te]));
+    }
+    const int base = ts - e0 + jt0;
+
+    // tile -> shared memory; survivor prefix in item order
+    for (int i = tid; i < kMergeTile; i += kMergeThreads) {
+        if (i < tlen) {
+            tkey[i] = okey[ts + i];
+            tslot[i] = slot_of(opt[ts + i]);
+        }
+    }
+    __syncthreads();
+    unsigned flags[4];
+    unsigned cnt = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int i = tid * 4 + k;
+        const bool surv = i < tlen && (init || tslot[i] < el || tslot[i] >= el + c);
+        flags[k] = surv ? 1u : 0u;
+        cnt += flags[k];
+    }
+    // 256-thread exclusive scan
+    {
+        const int lane = tid & 31, w = tid >> 5;
+        unsigned incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned x = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += x;
+        }
+        if (lane == 31) wsum[w] = incl;
+        __syncthreads();
+        if (w == 0) {
+            const unsigned x = lane < kMergeThreads / 32 ? wsum[lane] : 0u;
+            unsigned xi = x;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned y = __shfl_up_sync(kFull, xi, o);
+                if (lane >= o) xi += y;
+            }
+            if (lane < kMergeThreads / 32) wsum[lane] = xi - x;
+        }
+        __syncthreads();
+        unsigned pre = wsum[w] + incl - cnt;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            spre[tid * 4 + k] = (int)pre;
+            pre += flags[k];
+        }
+        if (tid == kMergeThreads - 1) spre[kMergeTile] = (int)pre;
+    }
+    __syncthreads();
+
+    // survivors (coalesced, item order i = tid + 256 k)
+    const int m = jt1 - jt0;
+    for (int i = tid; i < tlen; i += kMergeThreads) {
+        const int s = tslot[i];
+        if (!(init || s < el || s >= el + c)) continue;
+        const int lessnew = m > 0 ? count_words_less(v.nword + jt0, m, el, tkey[i], s) : 0;
+        const int o = base + spre[i] + lessnew;
+        if (o < 0 || o >= n_new) {
+            atomicOr(&v.ctl->err, kErrChunk);
+            continue;
+        }
+        dkey[o] = tkey[i];
+        dpt[o] = opt[ts + i];
+        dcnt[o] = ocnt[ts + i];
+        v.parent[s] = s;
+    }
+    // new entries of this tile
+    for (int q = jt0 + tid; q < jt1; q += kMergeThreads) {
+        const unsigned long long wd = v.nword[q];
+        const unsigned long long key = wd >> kOffBits;
+        const int slot = el + (int)(wd & ((1u << kOffBits) - 1));
+        int lo = 0, hi = tlen;  // old tile entries below (key, slot)
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (tuple_less(tkey[mid], tslot[mid], key, slot))
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        const int o = base + (q - jt0) + spre[lo];
+        if (o < 0 || o >= n_new || slot < 0 || slot >= v.W) {
+            atomicOr(&v.ctl->err, kErrChunk);
+            continue;
+        }
+        dkey[o] = key;
+        dpt[o] = v.ring[slot];
+        dcnt[o] = 0;
+        v.parent[slot] = slot;
+    }
+}
+
+// Cell table and work list of the new sorted window.  A work item is a
+// maximal run of one cell inside a 32-aligned block of sorted positions.
+__global__ void k_build(View v) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long b = v.ctl->b;
+    const int cur = (int)(b & 1);
+    const unsigned gen = gen_of_build(b);
+    const int n = v.ctl->nocc[cur];
+    const int i = gw * 32 + lane;
+    if (gw * 32 >= n) return;  // warp-uniform
+    const unsigned long long* skey = v.skey[cur];
+    const bool valid = i < n;
+    const unsigned long long k = valid ? skey[i] : ~0ull;
+    unsigned long long kp = __shfl_up_sync(kFull, k, 1);
+    unsigned long long kn = __shfl_down_sync(kFull, k, 1);
+    if (lane == 0) kp = i > 0 ? skey[i - 1] : ~0ull;
+    if (lane == 31) kn = (i + 1 < n) ? skey[i + 1] : ~0ull;
+    const bool first = valid && (i == 0 || kp != k);
+    const bool last = valid && (i == n - 1 || kn != k);
+    int err = 0;
+    ulonglong2* T = v.table[cur];
+    const unsigned long long tag = tag_of(k & kKeyMask, gen);
+    if (first && !table_set(T, v.pmask, v.pbits, tag, 0, i)) err |= kErrHashFull;
+    if (last && !table_set(T, v.pmask, v.pbits, tag, 1, i + 1)) err |= kErrHashFull;
+    const unsigned starts = __ballot_sync(kFull, valid && (first || lane == 0));
+    const unsigned nfirst = __popc(__ballot_sync(kFull, first));
+    int base = 0;
+    if (lane == 0) {
+        base = atomicAdd(&v.ctl->nitems, __popc(starts));
+        atomicAdd(&v.ctl->ncells, (int)nfirst);
+    }
+    base = __shfl_sync(kFull, base, 0);
+    if (valid && (first || lane == 0)) {
+        const int rank = __popc(starts & lanemask_lt(lane));
+        const unsigned above = starts & ~((2u << lane) - 1u);
+        const int next = above ? gw * 32 + __ffs(above) - 1 : gw * 32 + 32;
+        const int end = min(next, n);
+        if (base + rank < v.max_items)
+            v.items[base + rank] = make_int2(i, end - i);
+        else
+            err |= kErrItems;
+    }
+    if (err) atomicOr(&v.ctl->err, err);
+}
+
+// Full count of each new point and +1 on every older neighbour (new grid).
+template <int MODE, int DIM>
+__global__ void k_incr(View v, int j, int c, int init) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (gw >= c) return;
+    const long long b = v.ctl->b;
+    const int cur = (int)(b & 1);
+    const unsigned gen = gen_of_build(b);
+    const int el = chunk_base_slot(v, j, init);
+    const unsigned long long word = v.nword[gw];
+    const unsigned long long key = word >> kOffBits;
+    const int aslot = el + (int)(word & ((1u << kOffBits) - 1));
+    const float4 ap = v.ring[aslot];
+    int rs, re;
+    row_ranges<DIM>(v, v.table[cur], gen, key, lane, rs, re);
+    const float4* spt = v.spt[cur];
+    int* scnt = v.scnt[cur];
+    unsigned rechecks = 0;
+    int total = 0, mypos = -1;
+    constexpr int kRows = DIM == 1 ? 1 : (DIM == 2 ? 3 : 9);
+#pragma unroll 1
+    for (int r = 0; r < kRows; ++r) {
+        const int a = __shfl_sync(kFull, rs, r), e = __shfl_sync(kFull, re, r);
+        for (int base = a; base < e; base += 32) {
+            const int pos = base + lane;
+            bool nb = false;
+            if (pos < e) {
+                const float4 q = spt[pos];
+                const int qs = slot_of(q);
+                if (qs == aslot) {
+                    nb = true;
+                    mypos = pos;
+                } else if (is_nbr<MODE, DIM>(v, ap, q, rechecks)) {
+                    nb = true;
+                    if (qs < el || qs >= el + c) atomicAdd(&scnt[pos], 1);
+                }
+            }
+            total += __popc(__ballot_sync(kFull, nb));
+        }
+    }
+    mypos = __reduce_max_sync(kFull, (unsigned)(mypos + 1)) - 1;
+    int err = 0;
+    if (lane == 0) {
+        if (mypos >= 0)
+            scnt[mypos] = total;
+        else
+            err = kErrChunk;
+    }
+    flush_stats(v, rechecks, err, lane);
+}
+
+// Union of every core-core neighbour pair, each unordered pair once (the
+// candidate's sorted position is above the home point's).
+template <int MODE, int DIM>
+__global__ void k_union(View v) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const long long b = v.ctl->b;
+    const int cur = (int)(b & 1);
+    const unsigned gen = gen_of_build(b);
+    const int nitems = min(v.ctl->nitems, v.max_items);
+    const float4* spt = v.spt[cur];
+    const int* scnt = v.scnt[cur];
+    const unsigned long long* skey = v.skey[cur];
+    const ulonglong2* T = v.table[cur];
+    unsigned rechecks = 0;
+    int err = 0;
+    constexpr int kRows = DIM == 1 ? 1 : (DIM == 2 ? 3 : 9);
+    for (int itx = gw; itx < nitems; itx += nw) {
+        const int2 item = v.items[itx];
+        const int start = item.x, len = item.y;
+        const bool hv = lane < len;
+        float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
+        bool hcore = false;
+        if (hv) {
+            h = spt[start + lane];
+            hcore = scnt[start + lane] >= v.min_pts;
+        }
+        const unsigned hmask = __ballot_sync(kFull, hcore);
+        if (!hmask) continue;
+        const int hmin = start + __ffs(hmask) - 1;
+        int rs, re;
+        row_ranges<DIM>(v, T, gen, skey[start], lane, rs, re);
+#pragma unroll 1
+        for (int r = 0; r < kRows; ++r) {
+            const int a = max(__shfl_sync(kFull, rs, r), hmin + 1);
+            const int e = __shfl_sync(kFull, re, r);
+            for (int base = a; base < e; base += 32) {
+                const int pos = base + lane;
+                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                bool qc = false;
+                if (pos < e) {
+                    qc = scnt[pos] >= v.min_pts;
+                    if (qc) q = spt[pos];
+                }
+                if (!__any_sync(kFull, qc)) continue;
+                unsigned mm = hmask;
+                while (mm) {
+                    const int hi = __ffs(mm) - 1;
+                    mm &= mm - 1;
+                    const float4 hp = shfl_pt(h, hi);
+                    if (qc && pos > start + hi && is_nbr<MODE, DIM>(v, hp, q, rechecks))
+                        uf_unite(v.parent, slot_of(hp), slot_of(q), err);
+                }
+            }
+        }
+    }
+    flush_stats(v, rechecks, err, lane);
+}
+
+// Labels and ids by slot: core -> 0 and its root; non-core -> 1 and the
+// minimum root over adjacent cores, or 2 and its own slot.
+template <int MODE, int DIM>
+__global__ void k_label(View v, int advance) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const long long b = v.ctl->b;
+    const int cur = (int)(b & 1);
+    const unsigned gen = gen_of_build(b);
+    const int nitems = min(v.ctl->nitems, v.max_items);
+    const float4* spt = v.spt[cur];
+    const int* scnt = v.scnt[cur];
+    const unsigned long long* skey = v.skey[cur];
+    const ulonglong2* T = v.table[cur];
+    unsigned rechecks = 0;
+    constexpr int kRows = DIM == 1 ? 1 : (DIM == 2 ? 3 : 9);
+    for (int itx = gw; itx < nitems; itx += nw) {
+        const int2 item = v.items[itx];
+        const int start = item.x, len = item.y;
+        const bool hv = lane < len;
+        float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
+        bool hcore = false;
+        int hslot = -1;
+        if (hv) {
+            h = spt[start + lane];
+            hslot = slot_of(h);
+            hcore = scnt[start + lane] >= v.min_pts;
+            if (hcore) {
+                v.label[hslot] = 0;
+                v.cid[hslot] = uf_find(v.parent, hslot);
+            }
+        }
+        const unsigned nmask = __ballot_sync(kFull, hv && !hcore);
+        if (!nmask) continue;
+        int rs, re;
+        row_ranges<DIM>(v, T, gen, skey[start], lane, rs, re);
+        int best = INT_MAX;
+#pragma unroll 1
+        for (int r = 0; r < kRows; ++r) {
+            const int a = __shfl_sync(kFull, rs, r), e = __shfl_sync(kFull, re, r);
+            for (int base = a; base < e; base += 32) {
+                const int pos = base + lane;
+                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                bool qc = false;
+                if (pos < e) {
+                    qc = scnt[pos] >= v.min_pts;
+                    if (qc) q = spt[pos];
+                }
+                if (!__any_sync(kFull, qc)) continue;
+                int croot = -1;
+                unsigned mm = nmask;
+                while (mm) {
+                    const int hi = __ffs(mm) - 1;
+                    mm &= mm - 1;
+                    const float4 hp = shfl_pt(h, hi);
+                    int val = INT_MAX;
+                    if (qc && is_nbr<MODE, DIM>(v, hp, q, rechecks)) {
+                        if (croot < 0) croot = uf_find(v.parent, slot_of(q));
+                        val = croot;
+                    }
+                    const int mn = (int)__reduce_min_sync(kFull, (unsigned)val);
+                    if (lane == hi) best = min(best, mn);
+                }
+            }
+        }
+        if (hv && !hcore) {
+            if (best != INT_MAX) {
+                v.label[hslot] = 1;
+                v.cid[hslot] = best;
+            } else {
+                v.label[hslot] = 2;
+                v.cid[hslot] = hslot;
+            }
+        }
+    }
+    flush_stats(v, rechecks, 0, lane);
+    if (advance && blockIdx.x == 0 && threadIdx.x == 0) v.ctl->slide += 1;  // no reader here
+}
+
+__global__ void k_counts_by_slot(View v, int* nn) {
+    const int cur = (int)(v.ctl->b & 1);
+    const int n = v.ctl->nocc[cur];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        nn[slot_of(v.spt[cur][i])] = v.scnt[cur][i];
+}
+
+int g_num_sms = 0;
+
+}  // namespace
+
+#define RTDBS_DISPATCH(prec, dim, KERNEL, GRID, BLOCK, STREAM, ...)           \
+    do {                                                                         \
+        if ((prec) == kPrecFp32) {                                               \
+            if ((dim) == 1) KERNEL<kPrecFp32, 1><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);      \
+            else if ((dim) == 2) KERNEL<kPrecFp32, 2><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); \
+            else KERNEL<kPrecFp32, 3><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);                 \
+        } else {                                                                 \
+            if ((dim) == 1) KERNEL<kPrecFp64, 1><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);      \
+            else if ((dim) == 2) KERNEL<kPrecFp64, 2><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); \
+            else KERNEL<kPrecFp64, 3><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);                 \
+        }                                                                        \
+    } while (0)
+
+static constexpr size_t kSortSmem = sizeof(unsigned long long) * kChunkMax + sizeof(unsigned) * 256 * 32;
+
+cudaError_t configure_kernels() {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSortSmem);
+}
+
+cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, int init,
+                         int stg_off, int advance, cudaStream_t s) {
+    const int warp_blocks = (c * 32 + 255) / 256;
+    switch (phase) {
+        case kPhaseIngest:
+            k_ingest<<<(c + 255) / 256, 256, 0, s>>>(v, j, c, init, stg_off);
+            break;
+        case kPhaseSort:
+            k_sort<<<init ? 1 : 2, kSortThreads, kSortSmem, s>>>(v, c, init);
+            break;
+        case kPhaseDecrement:
+            if (!init) RTDBS_DISPATCH(precision, v.dim, k_decr, warp_blocks, 256, s, v, j, c);
+            break;
+        case kPhaseMerge:
+            k_merge<<<(v.W + kMergeTile - 1) / kMergeTile, kMergeThreads, 0, s>>>(v, j, c, init);
+            break;
+        case kPhaseBuild:
+            k_build<<<(v.W + 255) / 256, 256, 0, s>>>(v);
+            break;
+        case kPhaseIncrement:
+            RTDBS_DISPATCH(precision, v.dim, k_incr, warp_blocks, 256, s, v, j, c, init);
+            break;
+        case kPhaseUnion:
+        case kPhaseLabel: {
+            const int sms = g_num_sms > 0 ? g_num_sms : 152;
+            const int need = (v.max_items + 7) / 8;  // at most one warp per work item
+            const int blocks = max(1, min(sms * 8, need));
+            if (phase == kPhaseUnion)
+                RTDBS_DISPATCH(precision, v.dim, k_union, blocks, 256, s, v);
+            else
+                RTDBS_DISPATCH(precision, v.dim, k_label, blocks, 256, s, v, advance);
+            break;
+        }
+        default:
+            return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_chunk_step(const View& v, int precision, int j, int c, int init, int stg_off,
+                              cudaStream_t s) {
+    if (c <= 0 || c > kChunkMax) return cudaErrorInvalidValue;
+    for (int ph = 0; ph < kChunkPhases; ++ph) {
+        const cudaError_t e = launch_phase(ph, v, precision, j, c, init, stg_off, 0, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_cluster(const View& v, int precision, int advance, cudaStream_t s) {
+    cudaError_t e = launch_phase(kPhaseUnion, v, precision, 0, 0, 0, 0, advance, s);
+    if (e == cudaSuccess) e = launch_phase(kPhaseLabel, v, precision, 0, 0, 0, 0, advance, s);
+    return e;
+}
+
+cudaError_t launch_counts_by_slot(const View& v, int* nn, cudaStream_t s) {
+    const int sms = g_num_sms > 0 ? g_num_sms : 152;
+    k_counts_by_slot<<<sms * 4, 256, 0, s>>>(v, nn);
+    return cudaGetLastError();
+}
+
+}  // namespace rtdbs

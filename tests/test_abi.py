@@ -1,0 +1,92 @@
+"""C-ABI checks that need no GPU: the library builds for sm_103a, loads, and
+exports every function include/rtdbs.h declares; argument validation and
+status reporting work without touching a device."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+from rtdbstream_gb300 import build as rbuild
+from rtdbstream_gb300 import engine as E
+
+
+def header_functions():
+    text = open(os.path.join(ROOT, "include", "rtdbs.h")).read()
+    return re.findall(r"RTDBS_API\s+[\w\s\*]+?\b(rtdbs_\w+)\s*\(", text)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return E.load_library()
+
+
+def test_header_declares_api():
+    names = header_functions()
+    assert "rtdbs_create" in names and "rtdbs_slide" in names
+    assert len(names) == len(set(names))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in header_functions():
+        assert hasattr(lib, name), name
+    assert set(header_functions()) == set(E.EXPORTED_SYMBOLS)
+
+
+def test_library_is_sm103a_build():
+    rbuild.build()
+    assert os.path.exists(rbuild.LIB)
+    assert "arch=compute_103a,code=sm_103a" in rbuild.ARCH
+
+
+def test_abi_version_and_status_strings(lib):
+    assert lib.rtdbs_abi_version() == 1
+    assert lib.rtdbs_status_string(0) == b"ok"
+    assert lib.rtdbs_status_string(-5) == b"device-side bound hit"
+
+
+def test_params_init_defaults(lib):
+    p = E.Params()
+    assert lib.rtdbs_params_init(ctypes.byref(p)) == 0
+    assert p.dim == 3 and p.precision == E.PREC_FP64 and p.has_bbox == 0
+
+
+@pytest.mark.parametrize("field,value", [("dim", 4), ("dim", 0), ("stride", 7), ("eps", 0.0),
+                                         ("eps", float("nan")), ("precision", 9), ("stride", 0)])
+def test_invalid_params_rejected_before_device(lib, field, value):
+    p = E.Params()
+    lib.rtdbs_params_init(ctypes.byref(p))
+    p.dim, p.window, p.stride, p.min_pts, p.eps = 2, 100, 10, 4, 0.5
+    setattr(p, field, value)
+    h = ctypes.c_void_p()
+    rc = lib.rtdbs_create(ctypes.byref(p), None, ctypes.byref(h))
+    assert rc == E.RTDBS_ERR_INVALID
+    assert lib.rtdbs_last_error() != b""
+    assert not h.value
+
+
+def test_null_arguments(lib):
+    assert lib.rtdbs_create(None, None, None) == E.RTDBS_ERR_INVALID
+    assert lib.rtdbs_slide(None, None, None, None) == E.RTDBS_ERR_INVALID
+    assert lib.rtdbs_destroy(None) == 0
+
+
+def test_create_without_device_fails_cleanly(lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    p = E.Params()
+    lib.rtdbs_params_init(ctypes.byref(p))
+    p.dim, p.window, p.stride, p.min_pts, p.eps = 2, 100, 10, 4, 0.5
+    h = ctypes.c_void_p()
+    assert lib.rtdbs_create(ctypes.byref(p), None, ctypes.byref(h)) == E.RTDBS_ERR_NO_DEVICE
+
+
+def test_engine_raises_without_device():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(E.RtdbsError):
+        E.Engine(2, 100, 10, 0.5, 4)

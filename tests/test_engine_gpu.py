@@ -1,0 +1,204 @@
+"""GPU parity of the engine, called through the C ABI, against the CPU oracle
+and against fixtures produced by the reference's own cluster_with_cpu.
+
+Integer results are compared bit-exactly: neighbour counts, labels and
+cluster ids (noise ids are the point's own slot by definition).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden_files, load_golden
+
+import oracle as O
+from rtdbstream_gb300 import Engine, RtdbsError
+from rtdbstream_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    O.build(ref=False)
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+
+
+def run_stream(points, W, S, eps, mp, n_slides, precision="fp64", use_graph=True, bbox=None):
+    eng = Engine(points.shape[1], W, S, eps, mp, precision=precision, use_graph=use_graph, bbox=bbox)
+    eng.load_window(points[:W])
+    labs, cids, nns = [], [], []
+    for k in range(n_slides):
+        lab, cid = eng.slide(points[W + k * S: W + (k + 1) * S])
+        labs.append(lab)
+        cids.append(cid)
+        nns.append(eng.counts())
+    st = eng.stats()
+    eng.close()
+    return np.array(nns), np.array(labs), np.array(cids), st
+
+
+def assert_same(got, exp, what=""):
+    nn, lab, cid = got
+    enn, elab, ecid = exp
+    assert np.array_equal(nn, enn), f"{what}: counts differ at {np.argwhere(nn != enn)[:5].tolist()}"
+    assert np.array_equal(lab, elab), f"{what}: labels differ at {np.argwhere(lab != elab)[:5].tolist()}"
+    keep = elab != 2
+    assert np.array_equal(cid[keep], ecid[keep]), f"{what}: ids differ"
+    assert np.array_equal(np.where(lab == 2, cid, -1),
+                          np.where(lab == 2, np.broadcast_to(np.arange(lab.shape[-1]), lab.shape), -1))
+
+
+@pytest.mark.parametrize("path", golden_files("window"), ids=os.path.basename)
+def test_window_fp32_matches_reference_golden(path):
+    g = load_golden(path)
+    pts = g["pts"]
+    W = len(pts)
+    eng = Engine(pts.shape[1], W, W, float(g["eps"]), int(g["min_pts"]), precision="fp32")
+    eng.load_window(pts)
+    lab, cid = eng.cluster()
+    nn = eng.counts()
+    eng.close()
+    assert_same((nn, lab, cid), (g["nn"], g["label"], g["cid"]), os.path.basename(path))
+
+
+@pytest.mark.parametrize("path", golden_files("stream"), ids=os.path.basename)
+def test_stream_fp32_matches_reference_golden(path):
+    g = load_golden(path)
+    W, S = int(g["W"]), int(g["S"])
+    slides = g["nn"].shape[0]
+    got = run_stream(g["pts"], W, S, float(g["eps"]), int(g["min_pts"]), slides, precision="fp32")
+    assert_same(got[:3], (g["nn"], g["label"], g["cid"]), os.path.basename(path))
+
+
+@pytest.mark.parametrize("path", golden_files("stream"), ids=os.path.basename)
+def test_stream_fp64_matches_oracle(path):
+    g = load_golden(path)
+    W, S = int(g["W"]), int(g["S"])
+    slides = g["nn"].shape[0]
+    eps, mp = float(g["eps"]), int(g["min_pts"])
+    got = run_stream(g["pts"], W, S, eps, mp, slides, precision="fp64")
+    exp = O.stream(g["pts"], W, S, eps, mp, O.MODE_FP64, first_slide=1, n_out=slides)
+    assert_same(got[:3], exp, os.path.basename(path))
+
+
+CASES = [
+    # name, points, W, S, eps, min_pts, slides
+    ("mix2d_W10k_S1k", lambda: wl.gaussian_mixture(10_000 + 6 * 1_000, dim=2, seed=3), 10_000, 1_000, 0.5, 5, 6),
+    ("walk3d_W60k_S6k", lambda: wl.random_walkers(60_000 + 4 * 6_000, n_walkers=300, seed=4), 60_000, 6_000,
+     3.3e-3, 10, 4),
+    ("band3d_W20k_S2k", lambda: wl.offset_band_points(20_000 + 4 * 2_000, 1e-3, partner_frac=0.3, seed=5),
+     20_000, 2_000, 1e-3, 2, 4),
+    ("stk1d_W8k_S2k", lambda: wl.gaussian_mixture(8_000 + 3 * 2_000, dim=1, k=6, box=10.0, sigma=0.3, seed=6),
+     8_000, 2_000, 0.01, 4, 3),
+    ("big_stride_W40k_S20k", lambda: wl.gaussian_mixture(40_000 + 3 * 20_000, dim=2, k=30, box=100.0, seed=7),
+     40_000, 20_000, 0.4, 6, 3),
+    ("S_eq_W_3d", lambda: wl.gaussian_mixture(3_000 * 4, dim=3, k=6, box=15.0, seed=8), 3_000, 3_000, 1.0, 5, 3),
+]
+
+
+@pytest.mark.parametrize("name,gen,W,S,eps,mp,slides", CASES, ids=[c[0] for c in CASES])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_streams_match_oracle(name, gen, W, S, eps, mp, slides, precision):
+    pts = gen()
+    got = run_stream(pts, W, S, eps, mp, slides, precision=precision)
+    mode = O.MODE_FP64 if precision == "fp64" else O.MODE_FP32
+    exp = O.stream(pts, W, S, eps, mp, mode, first_slide=1, n_out=slides)
+    assert_same(got[:3], exp, f"{name}/{precision}")
+    if name.startswith("band") and precision == "fp64":
+        assert got[3]["band_rechecks"] > 0
+        # the FP64 relation really differs from the reference's FP32 one here
+        e32 = O.stream(pts, W, S, eps, mp, O.MODE_FP32, first_slide=1, n_out=slides)
+        assert not np.array_equal(exp[0], e32[0])
+
+
+def test_graph_and_direct_launch_identical():
+    pts = wl.gaussian_mixture(5_000 + 5 * 500, dim=2, k=10, box=40.0, seed=9)
+    a = run_stream(pts, 5_000, 500, 0.5, 5, 5, use_graph=True)
+    b = run_stream(pts, 5_000, 500, 0.5, 5, 5, use_graph=False)
+    for x, y in zip(a[:3], b[:3]):
+        assert np.array_equal(x, y)
+
+
+def test_bbox_given_equals_bbox_from_first_window():
+    pts = wl.gaussian_mixture(4_000 + 4 * 1_000, dim=2, k=8, box=30.0, seed=10)
+    bbox = (pts.min(axis=0), pts.max(axis=0))
+    a = run_stream(pts, 4_000, 1_000, 0.5, 5, 4, bbox=bbox)
+    b = run_stream(pts, 4_000, 1_000, 0.5, 5, 4)
+    for x, y in zip(a[:3], b[:3]):
+        assert np.array_equal(x, y)
+
+
+def test_points_outside_bbox_are_exact():
+    """A stream that drifts far outside the given box is clamped into
+    boundary cells and must still be exact."""
+    pts = wl.gaussian_mixture(3_000 + 3 * 1_000, dim=2, k=6, box=20.0, seed=11)
+    pts[3_000:] += np.float32(50.0)
+    bbox = ((0.0, 0.0), (20.0, 20.0))
+    got = run_stream(pts, 3_000, 1_000, 0.5, 4, 3, bbox=bbox)
+    exp = O.stream(pts, 3_000, 1_000, 0.5, 4, O.MODE_FP64, first_slide=1, n_out=3)
+    assert_same(got[:3], exp, "drift")
+
+
+def test_duplicates_and_nonfinite_points():
+    rng = np.random.default_rng(12)
+    base = np.repeat(rng.uniform(0, 5, (20, 2)), 40, axis=0).astype(np.float32)
+    pts = np.concatenate([base, rng.uniform(0, 5, (400, 2)).astype(np.float32)])
+    pts = pts[rng.permutation(len(pts))]
+    pts[7] = np.nan
+    pts[11] = np.inf
+    W, S = 800, 200
+    got = run_stream(pts, W, S, 0.3, 4, 2)
+    exp = O.stream(pts, W, S, 0.3, 4, O.MODE_FP64, first_slide=1, n_out=2)
+    assert_same(got[:3], exp, "dups/nonfinite")
+
+
+def test_determinism_repeated_runs():
+    pts = wl.random_walkers(30_000 + 3 * 3_000, n_walkers=200, seed=13)
+    a = run_stream(pts, 30_000, 3_000, 3.3e-3, 8, 3)
+    b = run_stream(pts, 30_000, 3_000, 3.3e-3, 8, 3)
+    for x, y in zip(a[:3], b[:3]):
+        assert np.array_equal(x, y)
+
+
+def test_slide_async_device_buffers():
+    torch = pytest.importorskip("torch")
+    pts = wl.gaussian_mixture(6_000 + 3 * 2_000, dim=2, k=10, box=40.0, seed=14)
+    W, S = 6_000, 2_000
+    eng = Engine(2, W, S, 0.5, 5)
+    dev = torch.from_numpy(pts).cuda()
+    eng.load_window(dev[:W].contiguous())
+    lab = torch.empty(W, dtype=torch.int32, device="cuda")
+    cid = torch.empty(W, dtype=torch.int32, device="cuda")
+    exp = O.stream(pts, W, S, 0.5, 5, O.MODE_FP64, first_slide=1, n_out=3)
+    for k in range(3):
+        eng.slide_async(dev[W + k * S: W + (k + 1) * S].contiguous(), lab, cid)
+        eng.sync()
+        assert np.array_equal(lab.cpu().numpy(), exp[1][k])
+        keep = exp[1][k] != 2
+        assert np.array_equal(cid.cpu().numpy()[keep], exp[2][k][keep])
+    eng.close()
+
+
+def test_api_errors():
+    with pytest.raises(RtdbsError) as ei:
+        Engine(2, 100, 30, 0.5, 4)
+    assert ei.value.status == -1
+    eng = Engine(2, 100, 20, 0.5, 4)
+    with pytest.raises(RtdbsError) as ei:
+        eng.slide(np.zeros((20, 2), np.float32))
+    assert ei.value.status == -4
+    eng.close()
+
+
+def test_walkers_full_window_exact():
+    """The 1M-point walker window (the benchmark workload), two slides,
+    compared bit-exactly with the FP64 oracle."""
+    spec = wl.CFG1
+    pts = wl.cfg1_stream(n_total=spec.window + 2 * spec.stride)
+    got = run_stream(pts, spec.window, spec.stride, spec.eps, spec.min_pts, 2)
+    exp = O.stream(pts, spec.window, spec.stride, spec.eps, spec.min_pts, O.MODE_FP64, first_slide=1, n_out=2)
+    assert_same(got[:3], exp, "walkers 1M")
