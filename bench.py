@@ -84,9 +84,12 @@ def cpu_reference_sample(points: np.ndarray, threads: int, budget_s: float = 12.
         oracle.window_bruteforce(win, SPEC.eps, SPEC.min_pts)
         return time.perf_counter() - t0
 
+    avail = (len(points) - W) // S
+    if avail < 1:
+        raise ValueError("stream too short for one slide")
     t1 = one(1)
     rounds = max(1, int(budget_s / max(t1, 1e-3)))
-    jobs = [2 + (i % 50) for i in range(rounds * threads)]
+    jobs = [1 + (i % avail) for i in range(rounds * threads)]
     t0 = time.perf_counter()
     with cf.ThreadPoolExecutor(max_workers=threads) as ex:
         per = list(ex.map(one, jobs))
@@ -192,7 +195,8 @@ def algorithmic_bytes(phase: str, W: int, S: int, dim: int, cells: int, items: i
         "build": W * 8 + cells * 32 + items * 8,
         "increment": c * (8 + 16) + c * 4,
         "union": W * (16 + 4 + 4 + 4),
-        "label": W * (16 + 4 + 4 + 8),
+        "flatten": W * (16 + 4 + 4 + 4),
+        "label": W * (16 + 4 + 8),
     }[phase]
 
 
@@ -234,7 +238,11 @@ def run_ours(args) -> None:
     total_steps = args.warmup + args.steps + args.e2e_steps + args.profile_steps
     pts = wl.cfg1_stream(seed=1 + rank, n_total=W + total_steps * S)
     d_pts = torch.from_numpy(pts).to(f"cuda:{dev}")
-    stream = torch.cuda.current_stream()
+    # One dedicated stream for the engine, the timing events and the L2 flush
+    # (torch's default stream is the legacy NULL stream, which the engine
+    # would replace by a private stream of its own).
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
     eng = Engine(3, W, S, SPEC.eps, SPEC.min_pts, precision="fp64", device=dev,
                  stream=stream.cuda_stream)
     eng.load_window(pts[:W])
@@ -295,7 +303,7 @@ def run_ours(args) -> None:
         prof.append(eng.slide_profiled(new_pts(step)))
         step += 1
     st = eng.stats()
-    phases = ["ingest", "sort", "decrement", "merge", "build", "increment", "union", "label"]
+    phases = ["ingest", "sort", "decrement", "merge", "build", "increment", "union", "flatten", "label"]
     avg = {p: statistics.mean(x[f"{p}_ms"] for x in prof) for p in phases} if prof else {}
     verified = None
     if rank == 0 and not args.no_verify:
@@ -317,7 +325,7 @@ def run_ours(args) -> None:
     dom = max(avg, key=avg.get) if avg else None
     roofline = None
     if dom:
-        launches = st["chunks_per_slide"] if dom not in ("union", "label") else 1
+        launches = st["chunks_per_slide"] if dom not in ("union", "flatten", "label") else 1
         alg = algorithmic_bytes(dom, W, S, 3, st["cells"], st["work_items"]) * launches
         achieved = alg / (avg[dom] / 1000.0) / 1e9
         slide_alg = sum(algorithmic_bytes(p, W, S, 3, st["cells"], st["work_items"]) for p in phases)

@@ -114,6 +114,7 @@ typedef struct rtdbs_phase_times {
     float build_ms;       /* cell table + work list */
     float increment_ms;   /* counts of new points, +1 on their neighbours */
     float union_ms;       /* union-find over core pairs */
+    float flatten_ms;     /* root of every core point */
     float label_ms;       /* labels, ids, border rule */
     float total_ms;       /* first launch to last */
     int32_t chunks;

@@ -193,6 +193,7 @@ int allocate(rtdbs_engine* e) {
         {(void**)&v.table[1], sizeof(ulonglong2) * P},
         {(void**)&v.items, sizeof(int2) * v.max_items},
         {(void**)&v.parent, sizeof(int) * W},
+        {(void**)&v.sroot, sizeof(int) * W},
         {(void**)&v.label, sizeof(int) * W},
         {(void**)&v.cid, sizeof(int) * W},
         {(void**)&v.nsort, sizeof(unsigned long long) * C},
@@ -522,7 +523,7 @@ int rtdbs_get_stats(rtdbs_engine* e, rtdbs_stats* s) {
     s->device_bytes = (int64_t)e->dev_bytes;
     const int nchunks = (e->p.stride + e->chunk - 1) / e->chunk;
     s->chunks_per_slide = nchunks;
-    s->launches_per_slide = nchunks * rtdbs::kChunkPhases + 2;
+    s->launches_per_slide = nchunks * rtdbs::kChunkPhases + 3;
     return RTDBS_OK;
 }
 
@@ -533,7 +534,7 @@ int rtdbs_slide_profiled(rtdbs_engine* e, const float* d_new_points, rtdbs_phase
     CUDA_TRY(guard.err);
     const int S = e->p.stride, C = e->chunk;
     const int nchunks = (S + C - 1) / C;
-    const int nev = nchunks * rtdbs::kChunkPhases + 3;
+    const int nev = nchunks * rtdbs::kChunkPhases + 4;
     std::vector<cudaEvent_t> ev(nev, nullptr);
     for (auto& x : ev) CUDA_TRY(cudaEventCreate(&x));
     int rc = RTDBS_OK;
@@ -582,6 +583,7 @@ int rtdbs_slide_profiled(rtdbs_engine* e, const float* d_new_points, rtdbs_phase
         t->build_ms = ph[rtdbs::kPhaseBuild];
         t->increment_ms = ph[rtdbs::kPhaseIncrement];
         t->union_ms = ph[rtdbs::kPhaseUnion];
+        t->flatten_ms = ph[rtdbs::kPhaseFlatten];
         t->label_ms = ph[rtdbs::kPhaseLabel];
         t->total_ms = total;
         t->chunks = nchunks;

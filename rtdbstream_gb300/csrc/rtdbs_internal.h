@@ -14,6 +14,7 @@
 //                         (replaces the OptiX BVH, src/dbscan/optix.cpp:438-483)
 //   items  int2[W+W/32+64] work list: runs of <= 32 sorted points of one cell
 //   parent i32[W]         union-find forest by slot (reference: cluster_id)
+//   sroot  i32[W]         root of each sorted position after the union (-1: not core)
 //   label, cid i32[W]     outputs by slot
 //   chunk scratch: sort words, expired points.
 #pragma once
@@ -31,6 +32,8 @@ constexpr unsigned kGenMod = 16383;  // table generations 1..16383 (tag = gen <<
 constexpr int kMergeTile = 1024;   // old entries per merge block
 constexpr int kMergeThreads = 256;
 constexpr int kSortThreads = 1024;
+constexpr int kBuildThreads = 512;
+constexpr int kClusterThreads = 256;
 constexpr int kMaxIter = 1 << 20;  // bound on every device-side retry loop
 
 // Bits of Ctl::err.
@@ -83,6 +86,7 @@ struct View {
     ulonglong2* table[2];
     int2* items;
     int* parent;
+    int* sroot;                  // root of each sorted position (-1: not core)
     int* label;
     int* cid;
     unsigned long long* nsort;   // chunk sort words in (key << 14 | offset)
@@ -103,6 +107,7 @@ enum Phase : int {
     kPhaseBuild,
     kPhaseIncrement,
     kPhaseUnion,
+    kPhaseFlatten,
     kPhaseLabel,
     kNumPhases
 };

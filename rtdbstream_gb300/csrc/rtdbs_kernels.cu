@@ -266,6 +266,24 @@ __device__ __forceinline__ void uf_unite(int* parent, int a, int b, int& err) {
     err |= kErrUnionIter;
 }
 
+// Links the sets of a and b (any ancestors of the two points) by hooking the
+// larger root under the smaller; returns an ancestor of both afterwards.
+__device__ __forceinline__ int uf_link(int* parent, int a, int b, int& err) {
+    for (int it = 0; it < kMaxIter; ++it) {
+        if (a == b) return a;
+        if (a < b) {
+            const int t = a;
+            a = b;
+            b = t;
+        }
+        const int old = atomicCAS(&parent[a], a, b);
+        if (old == a) return b;
+        a = uf_find(parent, old);
+    }
+    err |= kErrUnionIter;
+    return a < b ? a : b;
+}
+
 __device__ __forceinline__ void flush_stats(const View& v, unsigned rechecks, int err, int lane) {
     unsigned r = rechecks;
 #pragma unroll
@@ -334,8 +352,8 @@ __device__ __forceinline__ unsigned block_excl_scan_1024(unsigned val, unsigned*
 
 // One-CTA stable LSD radix sort (8-bit digits over the key bits of the sort
 // word) of c <= 16384 words; block 0 sorts the new words, block 1 the
-// expired ones.  Warp-level multisplit: lanes with equal digits are ranked by
-// __match_any_sync; per-(digit, warp) counters are scanned in digit-major
+// expired ones.  Warp-level multisplit: lanes with equal digits are ranked
+// from eight ballots; per-(digit, warp) counters are scanned in digit-major
 // order so the order of equal digits is the item order.
 __global__ void __launch_bounds__(kSortThreads, 1) k_sort(View v, int c, int init) {
     extern __shared__ unsigned long long sort_smem[];
@@ -360,12 +378,23 @@ __global__ void __launch_bounds__(kSortThreads, 1) k_sort(View v, int c, int ini
         const int shift = kOffBits + 8 * pass;
         for (int i = tid; i < 256 * 32; i += kSortThreads) whist[i] = 0;
         __syncthreads();
+        // Rank of each item among the equal digits of its round (lanes with
+        // the same digit found with eight ballots), kept for the scatter.
+        unsigned info[16];
 #pragma unroll
         for (int r = 0; r < 16; ++r) {
+            info[r] = 0;
             if (r < ipt) {
                 const unsigned d = (unsigned)(it[r] >> shift) & 255u;
-                const unsigned peers = __match_any_sync(kFull, d);
-                if ((peers & lt) == 0) whist[d * 32 + w] += __popc(peers);
+                unsigned peers = kFull;
+#pragma unroll
+                for (int bit = 0; bit < 8; ++bit) {
+                    const unsigned bm = __ballot_sync(kFull, (d >> bit) & 1u);
+                    peers &= ((d >> bit) & 1u) ? bm : ~bm;
+                }
+                const unsigned rank = __popc(peers & lt), cnt = __popc(peers);
+                info[r] = rank | (cnt << 6);
+                if (rank == 0) whist[d * 32 + w] += cnt;  // this warp's column only
             }
         }
         __syncthreads();
@@ -387,12 +416,12 @@ __global__ void __launch_bounds__(kSortThreads, 1) k_sort(View v, int c, int ini
         for (int r = 0; r < 16; ++r) {
             if (r < ipt) {
                 const unsigned d = (unsigned)(it[r] >> shift) & 255u;
-                const unsigned peers = __match_any_sync(kFull, d);
+                const unsigned rank = info[r] & 63u, cnt = info[r] >> 6;
                 const unsigned base = whist[d * 32 + w];
                 __syncwarp();
-                if ((peers & lt) == 0) whist[d * 32 + w] = base + __popc(peers);
+                if (rank == 0) whist[d * 32 + w] = base + cnt;
                 __syncwarp();
-                buf[base + __popc(peers & lt)] = it[r];
+                buf[base + rank] = it[r];
             }
         }
         __syncthreads();
@@ -603,21 +632,24 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
 
 // Cell table and work list of the new sorted window.  A work item is a
 // maximal run of one cell inside a 32-aligned block of sorted positions.
-__global__ void k_build(View v) {
-    const int lane = threadIdx.x & 31;
+// Item and cell counters are reserved once per block.
+__global__ void __launch_bounds__(kBuildThreads) k_build(View v) {
+    __shared__ int wcount[kBuildThreads / 32];
+    __shared__ int wbase[kBuildThreads / 32];
+    __shared__ int bcells;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long b = v.ctl->b;
     const int cur = (int)(b & 1);
     const unsigned gen = gen_of_build(b);
     const int n = v.ctl->nocc[cur];
     const int i = gw * 32 + lane;
-    if (gw * 32 >= n) return;  // warp-uniform
     const unsigned long long* skey = v.skey[cur];
     const bool valid = i < n;
     const unsigned long long k = valid ? skey[i] : ~0ull;
     unsigned long long kp = __shfl_up_sync(kFull, k, 1);
     unsigned long long kn = __shfl_down_sync(kFull, k, 1);
-    if (lane == 0) kp = i > 0 ? skey[i - 1] : ~0ull;
+    if (lane == 0) kp = (valid && i > 0) ? skey[i - 1] : ~0ull;
     if (lane == 31) kn = (i + 1 < n) ? skey[i + 1] : ~0ull;
     const bool first = valid && (i == 0 || kp != k);
     const bool last = valid && (i == n - 1 || kn != k);
@@ -627,20 +659,30 @@ __global__ void k_build(View v) {
     if (first && !table_set(T, v.pmask, v.pbits, tag, 0, i)) err |= kErrHashFull;
     if (last && !table_set(T, v.pmask, v.pbits, tag, 1, i + 1)) err |= kErrHashFull;
     const unsigned starts = __ballot_sync(kFull, valid && (first || lane == 0));
-    const unsigned nfirst = __popc(__ballot_sync(kFull, first));
-    int base = 0;
-    if (lane == 0) {
-        base = atomicAdd(&v.ctl->nitems, __popc(starts));
-        atomicAdd(&v.ctl->ncells, (int)nfirst);
+    const int nfirst = __popc(__ballot_sync(kFull, first));
+    if (threadIdx.x == 0) bcells = 0;
+    if (lane == 0) wcount[wib] = __popc(starts);
+    __syncthreads();
+    if (lane == 0 && nfirst) atomicAdd(&bcells, nfirst);
+    if (threadIdx.x == 0) {
+        int tot = 0;
+        for (int w = 0; w < kBuildThreads / 32; ++w) {
+            wbase[w] = tot;
+            tot += wcount[w];
+        }
+        const int base = tot ? atomicAdd(&v.ctl->nitems, tot) : 0;
+        for (int w = 0; w < kBuildThreads / 32; ++w) wbase[w] += base;
     }
-    base = __shfl_sync(kFull, base, 0);
+    __syncthreads();
+    if (threadIdx.x == 0 && bcells) atomicAdd(&v.ctl->ncells, bcells);
     if (valid && (first || lane == 0)) {
         const int rank = __popc(starts & lanemask_lt(lane));
         const unsigned above = starts & ~((2u << lane) - 1u);
         const int next = above ? gw * 32 + __ffs(above) - 1 : gw * 32 + 32;
         const int end = min(next, n);
-        if (base + rank < v.max_items)
-            v.items[base + rank] = make_int2(i, end - i);
+        const int slot = wbase[wib] + rank;
+        if (slot < v.max_items)
+            v.items[slot] = make_int2(i, end - i);
         else
             err |= kErrItems;
     }
@@ -700,10 +742,15 @@ __global__ void k_incr(View v, int j, int c, int init) {
 }
 
 // Union of every core-core neighbour pair, each unordered pair once (the
-// candidate's sorted position is above the home point's).
+// candidate's sorted position is above the home point's).  A candidate's
+// root is found once per candidate chunk and compared with cached roots of
+// the home points (shared memory, per warp); a link is attempted only where
+// the two differ, so same-set pairs cost no memory traffic.
 template <int MODE, int DIM>
-__global__ void k_union(View v) {
+__global__ void __launch_bounds__(kClusterThreads, 4) k_union(View v) {
+    __shared__ int home_root[kClusterThreads / 32][32];
     const int lane = threadIdx.x & 31;
+    volatile int* rh = home_root[threadIdx.x >> 5];
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const long long b = v.ctl->b;
@@ -714,6 +761,7 @@ __global__ void k_union(View v) {
     const int* scnt = v.scnt[cur];
     const unsigned long long* skey = v.skey[cur];
     const ulonglong2* T = v.table[cur];
+    int* parent = v.parent;
     unsigned rechecks = 0;
     int err = 0;
     constexpr int kRows = DIM == 1 ? 1 : (DIM == 2 ? 3 : 9);
@@ -729,6 +777,8 @@ __global__ void k_union(View v) {
         }
         const unsigned hmask = __ballot_sync(kFull, hcore);
         if (!hmask) continue;
+        if (hcore) rh[lane] = reinterpret_cast<volatile int*>(parent)[slot_of(h)];
+        __syncwarp();
         const int hmin = start + __ffs(hmask) - 1;
         int rs, re;
         row_ranges<DIM>(v, T, gen, skey[start], lane, rs, re);
@@ -745,24 +795,55 @@ __global__ void k_union(View v) {
                     if (qc) q = spt[pos];
                 }
                 if (!__any_sync(kFull, qc)) continue;
+                unsigned adj = 0;
                 unsigned mm = hmask;
                 while (mm) {
                     const int hi = __ffs(mm) - 1;
                     mm &= mm - 1;
                     const float4 hp = shfl_pt(h, hi);
-                    if (qc && pos > start + hi && is_nbr<MODE, DIM>(v, hp, q, rechecks))
-                        uf_unite(v.parent, slot_of(hp), slot_of(q), err);
+                    if (qc && pos > start + hi && is_nbr<MODE, DIM>(v, hp, q, rechecks)) adj |= 1u << hi;
                 }
+                if (adj) {
+                    int rq = uf_find(parent, slot_of(q));
+                    while (adj) {
+                        const int hi = __ffs(adj) - 1;
+                        adj &= adj - 1;
+                        const int ra = rh[hi];
+                        if (ra != rq) {
+                            rq = uf_link(parent, ra, rq, err);
+                            rh[hi] = rq;
+                        }
+                    }
+                }
+                __syncwarp();
             }
         }
     }
     flush_stats(v, rechecks, err, lane);
 }
 
+// Root of every core point by sorted position (-1 for non-core points).
+__global__ void k_flatten(View v) {
+    const int cur = (int)(v.ctl->b & 1);
+    const int n = v.ctl->nocc[cur];
+    const float4* spt = v.spt[cur];
+    const int* scnt = v.scnt[cur];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int r = -1;
+        if (scnt[i] >= v.min_pts) r = uf_find(v.parent, slot_of(spt[i]));
+        v.sroot[i] = r;
+    }
+}
+
+__device__ __forceinline__ float4 shfl_xyz(const float4& p, int src) {
+    return make_float4(__shfl_sync(kFull, p.x, src), __shfl_sync(kFull, p.y, src),
+                       __shfl_sync(kFull, p.z, src), 0.f);
+}
+
 // Labels and ids by slot: core -> 0 and its root; non-core -> 1 and the
 // minimum root over adjacent cores, or 2 and its own slot.
 template <int MODE, int DIM>
-__global__ void k_label(View v, int advance) {
+__global__ void __launch_bounds__(kClusterThreads, 4) k_label(View v, int advance) {
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -771,7 +852,7 @@ __global__ void k_label(View v, int advance) {
     const unsigned gen = gen_of_build(b);
     const int nitems = min(v.ctl->nitems, v.max_items);
     const float4* spt = v.spt[cur];
-    const int* scnt = v.scnt[cur];
+    const int* sroot = v.sroot;
     const unsigned long long* skey = v.skey[cur];
     const ulonglong2* T = v.table[cur];
     unsigned rechecks = 0;
@@ -781,18 +862,17 @@ __global__ void k_label(View v, int advance) {
         const int start = item.x, len = item.y;
         const bool hv = lane < len;
         float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
-        bool hcore = false;
-        int hslot = -1;
+        int hslot = -1, hr = -1;
         if (hv) {
             h = spt[start + lane];
             hslot = slot_of(h);
-            hcore = scnt[start + lane] >= v.min_pts;
-            if (hcore) {
+            hr = sroot[start + lane];
+            if (hr >= 0) {
                 v.label[hslot] = 0;
-                v.cid[hslot] = uf_find(v.parent, hslot);
+                v.cid[hslot] = hr;
             }
         }
-        const unsigned nmask = __ballot_sync(kFull, hv && !hcore);
+        const unsigned nmask = __ballot_sync(kFull, hv && hr < 0);
         if (!nmask) continue;
         int rs, re;
         row_ranges<DIM>(v, T, gen, skey[start], lane, rs, re);
@@ -803,29 +883,24 @@ __global__ void k_label(View v, int advance) {
             for (int base = a; base < e; base += 32) {
                 const int pos = base + lane;
                 float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-                bool qc = false;
+                int qr = -1;
                 if (pos < e) {
-                    qc = scnt[pos] >= v.min_pts;
-                    if (qc) q = spt[pos];
+                    qr = sroot[pos];
+                    if (qr >= 0) q = spt[pos];
                 }
-                if (!__any_sync(kFull, qc)) continue;
-                int croot = -1;
+                if (!__any_sync(kFull, qr >= 0)) continue;
                 unsigned mm = nmask;
                 while (mm) {
                     const int hi = __ffs(mm) - 1;
                     mm &= mm - 1;
-                    const float4 hp = shfl_pt(h, hi);
-                    int val = INT_MAX;
-                    if (qc && is_nbr<MODE, DIM>(v, hp, q, rechecks)) {
-                        if (croot < 0) croot = uf_find(v.parent, slot_of(q));
-                        val = croot;
-                    }
+                    const float4 hp = shfl_xyz(h, hi);
+                    const int val = (qr >= 0 && is_nbr<MODE, DIM>(v, hp, q, rechecks)) ? qr : INT_MAX;
                     const int mn = (int)__reduce_min_sync(kFull, (unsigned)val);
                     if (lane == hi) best = min(best, mn);
                 }
             }
         }
-        if (hv && !hcore) {
+        if (hv && hr < 0) {
             if (best != INT_MAX) {
                 v.label[hslot] = 1;
                 v.cid[hslot] = best;
@@ -891,7 +966,7 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
             k_merge<<<(v.W + kMergeTile - 1) / kMergeTile, kMergeThreads, 0, s>>>(v, j, c, init);
             break;
         case kPhaseBuild:
-            k_build<<<(v.W + 255) / 256, 256, 0, s>>>(v);
+            k_build<<<(v.W + kBuildThreads - 1) / kBuildThreads, kBuildThreads, 0, s>>>(v);
             break;
         case kPhaseIncrement:
             RTDBS_DISPATCH(precision, v.dim, k_incr, warp_blocks, 256, s, v, j, c, init);
@@ -899,12 +974,18 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
         case kPhaseUnion:
         case kPhaseLabel: {
             const int sms = g_num_sms > 0 ? g_num_sms : 152;
-            const int need = (v.max_items + 7) / 8;  // at most one warp per work item
-            const int blocks = max(1, min(sms * 8, need));
+            const int per_block = kClusterThreads / 32;
+            const int need = (v.max_items + per_block - 1) / per_block;  // one warp per item at most
+            const int blocks = max(1, min(sms * 2048 / kClusterThreads, need));
             if (phase == kPhaseUnion)
-                RTDBS_DISPATCH(precision, v.dim, k_union, blocks, 256, s, v);
+                RTDBS_DISPATCH(precision, v.dim, k_union, blocks, kClusterThreads, s, v);
             else
-                RTDBS_DISPATCH(precision, v.dim, k_label, blocks, 256, s, v, advance);
+                RTDBS_DISPATCH(precision, v.dim, k_label, blocks, kClusterThreads, s, v, advance);
+            break;
+        }
+        case kPhaseFlatten: {
+            const int sms = g_num_sms > 0 ? g_num_sms : 152;
+            k_flatten<<<sms * 8, 256, 0, s>>>(v);
             break;
         }
         default:
@@ -924,8 +1005,9 @@ cudaError_t launch_chunk_step(const View& v, int precision, int j, int c, int in
 }
 
 cudaError_t launch_cluster(const View& v, int precision, int advance, cudaStream_t s) {
-    cudaError_t e = launch_phase(kPhaseUnion, v, precision, 0, 0, 0, 0, advance, s);
-    if (e == cudaSuccess) e = launch_phase(kPhaseLabel, v, precision, 0, 0, 0, 0, advance, s);
+    cudaError_t e = cudaSuccess;
+    for (int ph = kPhaseUnion; ph <= kPhaseLabel && e == cudaSuccess; ++ph)
+        e = launch_phase(ph, v, precision, 0, 0, 0, 0, advance, s);
     return e;
 }
 

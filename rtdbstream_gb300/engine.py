@@ -52,7 +52,7 @@ class Stats(ctypes.Structure):
                 ("reserved", ctypes.c_int64 * 3)]
 
 
-PHASES = ("ingest", "sort", "decrement", "merge", "build", "increment", "union", "label")
+PHASES = ("ingest", "sort", "decrement", "merge", "build", "increment", "union", "flatten", "label")
 
 
 class PhaseTimes(ctypes.Structure):
