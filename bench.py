@@ -54,7 +54,24 @@ def parse():
     ap.add_argument("--profile-steps", type=int, default=5)
     ap.add_argument("--no-verify", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    # smaller windows of the same walker stream, for profiler captures only
+    ap.add_argument("--window", type=int, default=None)
+    ap.add_argument("--stride", type=int, default=None)
+    args = ap.parse_args()
+    global SPEC, WORKLOAD
+    if args.window or args.stride:
+        W = args.window or SPEC.window
+        S = args.stride or SPEC.stride
+        SPEC = wl.StreamSpec(f"walkers3d-W{W}-S{S}", 3, W, S, SPEC.eps, SPEC.min_pts, SPEC.slides)
+        WORKLOAD = f"walkers3d W={W:,} S={S:,} Eps={SPEC.eps} MinPts={SPEC.min_pts} fp64"
+    return args
+
+
+def walker_stream(n_total: int, seed: int) -> np.ndarray:
+    """The walker stream; a smaller window keeps 500 points per walker trail
+    (2,000 walkers at W = 1M), so the local density matches the full size."""
+    walkers = max(1, round(2000 * SPEC.window / 1_000_000))
+    return wl.random_walkers(n_total, n_walkers=walkers, seed=seed)
 
 
 def dist_env():
@@ -108,7 +125,7 @@ def run_reference(args) -> None:
     world, rank, _ = dist_env()
     if rank != 0:
         return
-    pts = wl.cfg1_stream(n_total=SPEC.window + 60 * SPEC.stride)
+    pts = walker_stream(SPEC.window + 60 * SPEC.stride, seed=1)
     threads = os.cpu_count() or 1
     base = cpu_reference_sample(pts, threads)
     steps = max(1, args.steps)
@@ -236,7 +253,7 @@ def run_ours(args) -> None:
 
     W, S = SPEC.window, SPEC.stride
     total_steps = args.warmup + args.steps + args.e2e_steps + args.profile_steps
-    pts = wl.cfg1_stream(seed=1 + rank, n_total=W + total_steps * S)
+    pts = walker_stream(W + total_steps * S, seed=1 + rank)
     d_pts = torch.from_numpy(pts).to(f"cuda:{dev}")
     # One dedicated stream for the engine, the timing events and the L2 flush
     # (torch's default stream is the legacy NULL stream, which the engine

@@ -95,7 +95,8 @@ namespace {
 
 // Grid geometry: cell side L = Eps (1 + 2^-12) >= Eps (the margin covers the
 // rounding of both predicates and of the double cell coordinate), clamped
-// extents over the bounding box, L doubled until the key fits 50 bits.
+// extents over the bounding box, one bit field per axis in the key, L doubled
+// until the fields fit 50 bits.
 int set_geometry(rtdbs_engine* e, const float* bmin, const float* bmax, bool widen) {
     const int dim = e->p.dim;
     double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
@@ -112,28 +113,31 @@ int set_geometry(rtdbs_engine* e, const float* bmin, const float* bmax, bool wid
         }
     }
     long long ext[3] = {1, 1, 1};
+    int bits[3] = {0, 0, 0};
     for (int guard = 0; guard < 4096; ++guard) {
-        double prod = 1.0;
+        int total = 0;
         for (int a = 0; a < dim; ++a) {
             const double n = std::floor((hi[a] - lo[a]) / L) + 1.0;
-            ext[a] = (long long)n;
-            prod *= n;
+            ext[a] = n < 4.0e15 ? (long long)n : (long long)4.0e15;
+            bits[a] = 0;
+            while (bits[a] < 62 && (1ll << bits[a]) < ext[a]) ++bits[a];
+            total += bits[a];
         }
-        if (prod <= std::ldexp(1.0, rtdbs::kKeyBitsMax) - 1.0) break;
+        if (total <= rtdbs::kKeyBitsMax) break;
         L *= 2.0;
     }
-    unsigned long long prod = 1;
-    for (int a = 0; a < 3; ++a) prod *= (unsigned long long)ext[a];
-    int bits = 0;
-    while (bits < 64 && (1ull << bits) < prod) ++bits;
     View& v = e->v;
     for (int a = 0; a < 3; ++a) {
         v.origin[a] = lo[a];
         v.ext[a] = ext[a];
     }
+    v.shift[2] = 0;
+    v.shift[1] = bits[2];
+    v.shift[0] = bits[1] + bits[2];
+    const int kbits = bits[0] + bits[1] + bits[2];
     v.inv_cell = 1.0 / L;
-    v.key_bits = bits;
-    v.sort_passes = (bits + 7) / 8;
+    v.key_bits = kbits;
+    v.sort_passes = (kbits + 7) / 8;
     e->cell_side = L;
     e->geometry_ready = true;
     return RTDBS_OK;

@@ -59,11 +59,12 @@ struct Ctl {
 
 // Everything a kernel needs for one stream, passed by value.
 struct View {
-    // geometry: cell (i, j, k) = clamp(floor((x - origin) * inv_cell)),
-    // key = (i * ext[1] + j) * ext[2] + k
+    // geometry: cell (i, j, k) = clamp(floor((x - origin) * inv_cell), 0, ext - 1),
+    // key = i << shift[0] | j << shift[1] | k (bit fields, shift[2] = 0)
     double origin[3];
     double inv_cell;
     long long ext[3];
+    int shift[3];
     int dim;
     // parameters
     int W, S, min_pts, units;   // units = W / S

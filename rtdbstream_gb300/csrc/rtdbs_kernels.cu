@@ -65,7 +65,7 @@ __device__ __forceinline__ unsigned long long cell_key(const View& v, float x, f
             if (t > top) t = top;
             c = (long long)t;
         }
-        key = key * (unsigned long long)v.ext[a] + (unsigned long long)c;
+        key |= (unsigned long long)c << v.shift[a];
     }
     return key;
 }
@@ -187,11 +187,9 @@ template <int DIM>
 __device__ __forceinline__ void row_ranges(const View& v, const ulonglong2* T, unsigned gen,
                                            unsigned long long key, int lane, int& rs, int& re) {
     constexpr int kCells = DIM == 1 ? 3 : (DIM == 2 ? 9 : 27);
-    const long long e1 = v.ext[1], e2 = v.ext[2];
-    const long long c2 = (long long)(key % (unsigned long long)e2);
-    const long long rr = (long long)(key / (unsigned long long)e2);
-    const long long c1 = rr % e1;
-    const long long c0 = rr / e1;
+    const long long c2 = (long long)(key & ((1ull << v.shift[1]) - 1ull));
+    const long long c1 = (long long)((key >> v.shift[1]) & ((1ull << (v.shift[0] - v.shift[1])) - 1ull));
+    const long long c0 = (long long)(key >> v.shift[0]);
     int2 rg = make_int2(0, 0);
     if (lane < kCells) {
         long long q0 = c0, q1 = c1, q2 = c2;
@@ -205,11 +203,10 @@ __device__ __forceinline__ void row_ranges(const View& v, const ulonglong2* T, u
             q1 += (lane / 3) % 3 - 1;
             q2 += lane % 3 - 1;
         }
-        const bool ok = q0 >= 0 && q0 < v.ext[0] && q1 >= 0 && q1 < e1 && q2 >= 0 && q2 < e2;
+        const bool ok = q0 >= 0 && q0 < v.ext[0] && q1 >= 0 && q1 < v.ext[1] && q2 >= 0 && q2 < v.ext[2];
         if (ok) {
-            const unsigned long long nk =
-                ((unsigned long long)q0 * (unsigned long long)e1 + (unsigned long long)q1) *
-                    (unsigned long long)e2 + (unsigned long long)q2;
+            const unsigned long long nk = ((unsigned long long)q0 << v.shift[0]) |
+                                          ((unsigned long long)q1 << v.shift[1]) | (unsigned long long)q2;
             rg = table_find(T, v.pmask, v.pbits, tag_of(nk, gen));
         }
     }
@@ -227,6 +224,40 @@ __device__ __forceinline__ void row_ranges(const View& v, const ulonglong2* T, u
     if (e == INT_MIN) s = e = 0;
     rs = s;
     re = e;
+}
+
+// The warp's row ranges (lanes 0..kRows-1), clipped below at `lo`, laid end
+// to end: candidate idx in [0, total) lives at sorted position
+// start[r] + idx - pre[r] for the row r with pre[r] <= idx < pre[r+1].
+// Concatenating the rows keeps the 32-lane candidate chunks full.
+template <int DIM>
+__device__ __forceinline__ int candidate_stream(int rs, int re, int lo, int lane, int* sstart,
+                                                int* spre) {
+    constexpr int kRows = DIM == 1 ? 1 : (DIM == 2 ? 3 : 9);
+    const int a = max(rs, lo);
+    const int len = lane < kRows ? max(re - a, 0) : 0;
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 16; o <<= 1) {
+        const int t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(kFull, incl, kRows - 1);
+    __syncwarp();
+    if (lane < kRows) {
+        sstart[lane] = a;
+        spre[lane] = incl - len;
+    }
+    if (lane == 0) spre[kRows] = total;
+    __syncwarp();
+    return total;
+}
+
+// Sorted position of candidate idx; r is the lane's row cursor (rows only
+// advance as idx grows).
+__device__ __forceinline__ int stream_pos(int idx, int& r, const int* sstart, const int* spre) {
+    while (idx >= spre[r + 1]) ++r;
+    return sstart[r] + idx - spre[r];
 }
 
 // ---------------------------------------------------------------- union-find
@@ -247,27 +278,9 @@ __device__ __forceinline__ int uf_find(int* parent, int v) {
     return curr;
 }
 
-// Lock-free union: the larger root is hooked under the smaller one with
-// atomicCAS, so every root is the minimum slot of its set.
-__device__ __forceinline__ void uf_unite(int* parent, int a, int b, int& err) {
-    int ra = uf_find(parent, a);
-    int rb = uf_find(parent, b);
-    for (int it = 0; it < kMaxIter; ++it) {
-        if (ra == rb) return;
-        if (ra < rb) {
-            const int t = ra;
-            ra = rb;
-            rb = t;
-        }
-        const int old = atomicCAS(&parent[ra], ra, rb);
-        if (old == ra) return;
-        ra = uf_find(parent, old);
-    }
-    err |= kErrUnionIter;
-}
-
-// Links the sets of a and b (any ancestors of the two points) by hooking the
-// larger root under the smaller; returns an ancestor of both afterwards.
+// Lock-free union of the sets of a and b (any ancestors of the two points):
+// the larger root is hooked under the smaller with atomicCAS, so every root
+// is the minimum slot of its set.  Returns an ancestor of both afterwards.
 __device__ __forceinline__ int uf_link(int* parent, int a, int b, int& err) {
     for (int it = 0; it < kMaxIter; ++it) {
         if (a == b) return a;
@@ -439,8 +452,9 @@ __global__ void __launch_bounds__(kSortThreads, 1) k_sort(View v, int c, int ini
 
 // -1 on the count of every surviving neighbour of each expired point (old grid).
 template <int MODE, int DIM>
-__global__ void k_decr(View v, int j, int c) {
-    const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(256) k_decr(View v, int j, int c) {
+    __shared__ int rstart[8][9], rpre[8][10];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (gw >= c) return;
     const long long b = v.ctl->b;
@@ -452,22 +466,16 @@ __global__ void k_decr(View v, int j, int c) {
     const float4 xp = v.xpt[word & ((1u << kOffBits) - 1)];
     int rs, re;
     row_ranges<DIM>(v, v.table[old], gen, key, lane, rs, re);
+    const int total = candidate_stream<DIM>(rs, re, 0, lane, rstart[wib], rpre[wib]);
     const float4* spt = v.spt[old];
     int* scnt = v.scnt[old];
     unsigned rechecks = 0;
-    constexpr int kRows = DIM == 1 ? 1 : (DIM == 2 ? 3 : 9);
-#pragma unroll 1
-    for (int r = 0; r < kRows; ++r) {
-        const int a = __shfl_sync(kFull, rs, r), e = __shfl_sync(kFull, re, r);
-        for (int base = a; base < e; base += 32) {
-            const int pos = base + lane;
-            if (pos < e) {
-                const float4 q = spt[pos];
-                const int qs = slot_of(q);
-                if ((qs < el || qs >= el + c) && is_nbr<MODE, DIM>(v, xp, q, rechecks))
-                    atomicSub(&scnt[pos], 1);
-            }
-        }
+    int r = 0;
+    for (int idx = lane; idx < total; idx += 32) {
+        const int pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
+        const float4 q = spt[pos];
+        const int qs = slot_of(q);
+        if ((qs < el || qs >= el + c) && is_nbr<MODE, DIM>(v, xp, q, rechecks)) atomicSub(&scnt[pos], 1);
     }
     flush_stats(v, rechecks, 0, lane);
 }
@@ -691,8 +699,9 @@ __global__ void __launch_bounds__(kBuildThreads) k_build(View v) {
 
 // Full count of each new point and +1 on every older neighbour (new grid).
 template <int MODE, int DIM>
-__global__ void k_incr(View v, int j, int c, int init) {
-    const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(256) k_incr(View v, int j, int c, int init) {
+    __shared__ int rstart[8][9], rpre[8][10];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (gw >= c) return;
     const long long b = v.ctl->b;
@@ -705,36 +714,30 @@ __global__ void k_incr(View v, int j, int c, int init) {
     const float4 ap = v.ring[aslot];
     int rs, re;
     row_ranges<DIM>(v, v.table[cur], gen, key, lane, rs, re);
+    const int total = candidate_stream<DIM>(rs, re, 0, lane, rstart[wib], rpre[wib]);
     const float4* spt = v.spt[cur];
     int* scnt = v.scnt[cur];
     unsigned rechecks = 0;
-    int total = 0, mypos = -1;
-    constexpr int kRows = DIM == 1 ? 1 : (DIM == 2 ? 3 : 9);
-#pragma unroll 1
-    for (int r = 0; r < kRows; ++r) {
-        const int a = __shfl_sync(kFull, rs, r), e = __shfl_sync(kFull, re, r);
-        for (int base = a; base < e; base += 32) {
-            const int pos = base + lane;
-            bool nb = false;
-            if (pos < e) {
-                const float4 q = spt[pos];
-                const int qs = slot_of(q);
-                if (qs == aslot) {
-                    nb = true;
-                    mypos = pos;
-                } else if (is_nbr<MODE, DIM>(v, ap, q, rechecks)) {
-                    nb = true;
-                    if (qs < el || qs >= el + c) atomicAdd(&scnt[pos], 1);
-                }
-            }
-            total += __popc(__ballot_sync(kFull, nb));
+    int count = 0, mypos = -1, r = 0;
+    for (int idx = lane; idx < total; idx += 32) {
+        const int pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
+        const float4 q = spt[pos];
+        const int qs = slot_of(q);
+        if (qs == aslot) {
+            ++count;
+            mypos = pos;
+        } else if (is_nbr<MODE, DIM>(v, ap, q, rechecks)) {
+            ++count;
+            if (qs < el || qs >= el + c) atomicAdd(&scnt[pos], 1);
         }
     }
-    mypos = __reduce_max_sync(kFull, (unsigned)(mypos + 1)) - 1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) count += __shfl_xor_sync(kFull, count, o);
+    mypos = (int)__reduce_max_sync(kFull, (unsigned)(mypos + 1)) - 1;
     int err = 0;
     if (lane == 0) {
         if (mypos >= 0)
-            scnt[mypos] = total;
+            scnt[mypos] = count;
         else
             err = kErrChunk;
     }
@@ -745,18 +748,23 @@ __global__ void k_incr(View v, int j, int c, int init) {
 // candidate's sorted position is above the home point's).  A candidate's
 // root is found once per candidate chunk and compared with cached roots of
 // the home points (shared memory, per warp); a link is attempted only where
-// the two differ, so same-set pairs cost no memory traffic.
+// the two differ, so same-set pairs cost no memory traffic.  Each warp walks
+// a contiguous range of work items (neighbouring cells), so candidate loads
+// reuse L1.
 template <int MODE, int DIM>
-__global__ void __launch_bounds__(kClusterThreads, 4) k_union(View v) {
+__global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
     __shared__ int home_root[kClusterThreads / 32][32];
-    const int lane = threadIdx.x & 31;
-    volatile int* rh = home_root[threadIdx.x >> 5];
+    __shared__ int rstart[kClusterThreads / 32][9], rpre[kClusterThreads / 32][10];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    volatile int* rh = home_root[wib];
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const long long b = v.ctl->b;
     const int cur = (int)(b & 1);
     const unsigned gen = gen_of_build(b);
     const int nitems = min(v.ctl->nitems, v.max_items);
+    const int per = (nitems + nw - 1) / nw;
+    const int it0 = min(gw * per, nitems), it1 = min(it0 + per, nitems);
     const float4* spt = v.spt[cur];
     const int* scnt = v.scnt[cur];
     const unsigned long long* skey = v.skey[cur];
@@ -764,8 +772,7 @@ __global__ void __launch_bounds__(kClusterThreads, 4) k_union(View v) {
     int* parent = v.parent;
     unsigned rechecks = 0;
     int err = 0;
-    constexpr int kRows = DIM == 1 ? 1 : (DIM == 2 ? 3 : 9);
-    for (int itx = gw; itx < nitems; itx += nw) {
+    for (int itx = it0; itx < it1; ++itx) {
         const int2 item = v.items[itx];
         const int start = item.x, len = item.y;
         const bool hv = lane < len;
@@ -778,45 +785,43 @@ __global__ void __launch_bounds__(kClusterThreads, 4) k_union(View v) {
         const unsigned hmask = __ballot_sync(kFull, hcore);
         if (!hmask) continue;
         if (hcore) rh[lane] = reinterpret_cast<volatile int*>(parent)[slot_of(h)];
-        __syncwarp();
         const int hmin = start + __ffs(hmask) - 1;
         int rs, re;
         row_ranges<DIM>(v, T, gen, skey[start], lane, rs, re);
-#pragma unroll 1
-        for (int r = 0; r < kRows; ++r) {
-            const int a = max(__shfl_sync(kFull, rs, r), hmin + 1);
-            const int e = __shfl_sync(kFull, re, r);
-            for (int base = a; base < e; base += 32) {
-                const int pos = base + lane;
-                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-                bool qc = false;
-                if (pos < e) {
-                    qc = scnt[pos] >= v.min_pts;
-                    if (qc) q = spt[pos];
-                }
-                if (!__any_sync(kFull, qc)) continue;
-                unsigned adj = 0;
-                unsigned mm = hmask;
-                while (mm) {
-                    const int hi = __ffs(mm) - 1;
-                    mm &= mm - 1;
-                    const float4 hp = shfl_pt(h, hi);
-                    if (qc && pos > start + hi && is_nbr<MODE, DIM>(v, hp, q, rechecks)) adj |= 1u << hi;
-                }
-                if (adj) {
-                    int rq = uf_find(parent, slot_of(q));
-                    while (adj) {
-                        const int hi = __ffs(adj) - 1;
-                        adj &= adj - 1;
-                        const int ra = rh[hi];
-                        if (ra != rq) {
-                            rq = uf_link(parent, ra, rq, err);
-                            rh[hi] = rq;
-                        }
+        const int total = candidate_stream<DIM>(rs, re, hmin + 1, lane, rstart[wib], rpre[wib]);
+        int r = 0;
+        for (int base = 0; base < total; base += 32) {
+            const int idx = base + lane;
+            int pos = 0;
+            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+            bool qc = false;
+            if (idx < total) {
+                pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
+                qc = scnt[pos] >= v.min_pts;
+                if (qc) q = spt[pos];
+            }
+            if (!__any_sync(kFull, qc)) continue;
+            unsigned adj = 0;
+            unsigned mm = hmask;
+            while (mm) {
+                const int hi = __ffs(mm) - 1;
+                mm &= mm - 1;
+                const float4 hp = shfl_pt(h, hi);
+                if (qc && pos > start + hi && is_nbr<MODE, DIM>(v, hp, q, rechecks)) adj |= 1u << hi;
+            }
+            if (adj) {
+                int rq = uf_find(parent, slot_of(q));
+                while (adj) {
+                    const int hi = __ffs(adj) - 1;
+                    adj &= adj - 1;
+                    const int ra = rh[hi];
+                    if (ra != rq) {
+                        rq = uf_link(parent, ra, rq, err);
+                        rh[hi] = rq;
                     }
                 }
-                __syncwarp();
             }
+            __syncwarp();
         }
     }
     flush_stats(v, rechecks, err, lane);
@@ -843,21 +848,23 @@ __device__ __forceinline__ float4 shfl_xyz(const float4& p, int src) {
 // Labels and ids by slot: core -> 0 and its root; non-core -> 1 and the
 // minimum root over adjacent cores, or 2 and its own slot.
 template <int MODE, int DIM>
-__global__ void __launch_bounds__(kClusterThreads, 4) k_label(View v, int advance) {
-    const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advance) {
+    __shared__ int rstart[kClusterThreads / 32][9], rpre[kClusterThreads / 32][10];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const long long b = v.ctl->b;
     const int cur = (int)(b & 1);
     const unsigned gen = gen_of_build(b);
     const int nitems = min(v.ctl->nitems, v.max_items);
+    const int per = (nitems + nw - 1) / nw;
+    const int it0 = min(gw * per, nitems), it1 = min(it0 + per, nitems);
     const float4* spt = v.spt[cur];
     const int* sroot = v.sroot;
     const unsigned long long* skey = v.skey[cur];
     const ulonglong2* T = v.table[cur];
     unsigned rechecks = 0;
-    constexpr int kRows = DIM == 1 ? 1 : (DIM == 2 ? 3 : 9);
-    for (int itx = gw; itx < nitems; itx += nw) {
+    for (int itx = it0; itx < it1; ++itx) {
         const int2 item = v.items[itx];
         const int start = item.x, len = item.y;
         const bool hv = lane < len;
@@ -876,28 +883,26 @@ __global__ void __launch_bounds__(kClusterThreads, 4) k_label(View v, int advanc
         if (!nmask) continue;
         int rs, re;
         row_ranges<DIM>(v, T, gen, skey[start], lane, rs, re);
-        int best = INT_MAX;
-#pragma unroll 1
-        for (int r = 0; r < kRows; ++r) {
-            const int a = __shfl_sync(kFull, rs, r), e = __shfl_sync(kFull, re, r);
-            for (int base = a; base < e; base += 32) {
-                const int pos = base + lane;
-                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-                int qr = -1;
-                if (pos < e) {
-                    qr = sroot[pos];
-                    if (qr >= 0) q = spt[pos];
-                }
-                if (!__any_sync(kFull, qr >= 0)) continue;
-                unsigned mm = nmask;
-                while (mm) {
-                    const int hi = __ffs(mm) - 1;
-                    mm &= mm - 1;
-                    const float4 hp = shfl_xyz(h, hi);
-                    const int val = (qr >= 0 && is_nbr<MODE, DIM>(v, hp, q, rechecks)) ? qr : INT_MAX;
-                    const int mn = (int)__reduce_min_sync(kFull, (unsigned)val);
-                    if (lane == hi) best = min(best, mn);
-                }
+        const int total = candidate_stream<DIM>(rs, re, 0, lane, rstart[wib], rpre[wib]);
+        int best = INT_MAX, r = 0;
+        for (int base = 0; base < total; base += 32) {
+            const int idx = base + lane;
+            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+            int qr = -1;
+            if (idx < total) {
+                const int pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
+                qr = sroot[pos];
+                if (qr >= 0) q = spt[pos];
+            }
+            if (!__any_sync(kFull, qr >= 0)) continue;
+            unsigned mm = nmask;
+            while (mm) {
+                const int hi = __ffs(mm) - 1;
+                mm &= mm - 1;
+                const float4 hp = shfl_xyz(h, hi);
+                const int val = (qr >= 0 && is_nbr<MODE, DIM>(v, hp, q, rechecks)) ? qr : INT_MAX;
+                const int mn = (int)__reduce_min_sync(kFull, (unsigned)val);
+                if (lane == hi) best = min(best, mn);
             }
         }
         if (hv && hr < 0) {
@@ -976,7 +981,7 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
             const int sms = g_num_sms > 0 ? g_num_sms : 152;
             const int per_block = kClusterThreads / 32;
             const int need = (v.max_items + per_block - 1) / per_block;  // one warp per item at most
-            const int blocks = max(1, min(sms * 2048 / kClusterThreads, need));
+            const int blocks = max(1, min(sms * 6, need));
             if (phase == kPhaseUnion)
                 RTDBS_DISPATCH(precision, v.dim, k_union, blocks, kClusterThreads, s, v);
             else
