@@ -14,7 +14,8 @@
 //                         (replaces the OptiX BVH, src/dbscan/optix.cpp:438-483)
 //   items  int2[W+W/32+64] work list: runs of <= 32 sorted points of one cell
 //   parent i32[W]         union-find forest by slot (reference: cluster_id)
-//   sroot  i32[W]         root of each sorted position after the union (-1: not core)
+//   sroot  i32[W]         per sorted position: root hint during the union, then
+//                         the root (-1: not core)
 //   label, cid i32[W]     outputs by slot
 //   chunk scratch: sort words, expired points.
 #pragma once
@@ -87,7 +88,8 @@ struct View {
     ulonglong2* table[2];
     int2* items;
     int* parent;
-    int* sroot;                  // root of each sorted position (-1: not core)
+    int* sroot;                  // per sorted position: root hint during the union,
+                                 // then the root (-1: not core)
     int* label;
     int* cid;
     unsigned long long* nsort;   // chunk sort words in (key << 14 | offset)

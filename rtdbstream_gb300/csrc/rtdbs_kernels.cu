@@ -283,15 +283,15 @@ __device__ __forceinline__ int uf_find(int* parent, int v) {
 // is the minimum slot of its set.  Returns an ancestor of both afterwards.
 __device__ __forceinline__ int uf_link(int* parent, int a, int b, int& err) {
     for (int it = 0; it < kMaxIter; ++it) {
+        a = uf_find(parent, a);
+        b = uf_find(parent, b);
         if (a == b) return a;
         if (a < b) {
             const int t = a;
             a = b;
             b = t;
         }
-        const int old = atomicCAS(&parent[a], a, b);
-        if (old == a) return b;
-        a = uf_find(parent, old);
+        if (atomicCAS(&parent[a], a, b) == a) return b;
     }
     err |= kErrUnionIter;
     return a < b ? a : b;
@@ -611,6 +611,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
         dkey[o] = tkey[i];
         dpt[o] = opt[ts + i];
         dcnt[o] = ocnt[ts + i];
+        v.sroot[o] = s;
         v.parent[s] = s;
     }
     // new entries of this tile
@@ -634,6 +635,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
         dkey[o] = key;
         dpt[o] = v.ring[slot];
         dcnt[o] = 0;
+        v.sroot[o] = slot;
         v.parent[slot] = slot;
     }
 }
@@ -748,7 +750,8 @@ __global__ void __launch_bounds__(256) k_incr(View v, int j, int c, int init) {
 // candidate's sorted position is above the home point's).  A candidate's
 // root is found once per candidate chunk and compared with cached roots of
 // the home points (shared memory, per warp); a link is attempted only where
-// the two differ, so same-set pairs cost no memory traffic.  Each warp walks
+// the two differ, so same-set pairs cost no memory traffic.  Finds start
+// from per-position root hints.  Each warp walks
 // a contiguous range of work items (neighbouring cells), so candidate loads
 // reuse L1.
 template <int MODE, int DIM>
@@ -770,6 +773,10 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
     const unsigned long long* skey = v.skey[cur];
     const ulonglong2* T = v.table[cur];
     int* parent = v.parent;
+    // Root hints by sorted position (an ancestor of the point; the merge sets
+    // each to the point's own slot): coalesced with the candidate loads, and
+    // refreshed as roots are found, so find walks stay short.
+    volatile int* hint = v.sroot;
     unsigned rechecks = 0;
     int err = 0;
     for (int itx = it0; itx < it1; ++itx) {
@@ -784,7 +791,7 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
         }
         const unsigned hmask = __ballot_sync(kFull, hcore);
         if (!hmask) continue;
-        if (hcore) rh[lane] = reinterpret_cast<volatile int*>(parent)[slot_of(h)];
+        if (hcore) rh[lane] = hint[start + lane];
         const int hmin = start + __ffs(hmask) - 1;
         int rs, re;
         row_ranges<DIM>(v, T, gen, skey[start], lane, rs, re);
@@ -792,13 +799,16 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
         int r = 0;
         for (int base = 0; base < total; base += 32) {
             const int idx = base + lane;
-            int pos = 0;
+            int pos = 0, qh = 0;
             float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
             bool qc = false;
             if (idx < total) {
                 pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
                 qc = scnt[pos] >= v.min_pts;
-                if (qc) q = spt[pos];
+                if (qc) {
+                    q = spt[pos];
+                    qh = hint[pos];
+                }
             }
             if (!__any_sync(kFull, qc)) continue;
             unsigned adj = 0;
@@ -810,7 +820,7 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
                 if (qc && pos > start + hi && is_nbr<MODE, DIM>(v, hp, q, rechecks)) adj |= 1u << hi;
             }
             if (adj) {
-                int rq = uf_find(parent, slot_of(q));
+                int rq = uf_find(parent, qh);
                 while (adj) {
                     const int hi = __ffs(adj) - 1;
                     adj &= adj - 1;
@@ -820,24 +830,23 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
                         rh[hi] = rq;
                     }
                 }
+                if (rq != qh) hint[pos] = rq;
             }
             __syncwarp();
         }
+        if (hcore) hint[start + lane] = rh[lane];
     }
     flush_stats(v, rechecks, err, lane);
 }
 
-// Root of every core point by sorted position (-1 for non-core points).
+// Root of every core point by sorted position (-1 for non-core points),
+// walked from the position's root hint.
 __global__ void k_flatten(View v) {
     const int cur = (int)(v.ctl->b & 1);
     const int n = v.ctl->nocc[cur];
-    const float4* spt = v.spt[cur];
     const int* scnt = v.scnt[cur];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        int r = -1;
-        if (scnt[i] >= v.min_pts) r = uf_find(v.parent, slot_of(spt[i]));
-        v.sroot[i] = r;
-    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        v.sroot[i] = scnt[i] >= v.min_pts ? uf_find(v.parent, v.sroot[i]) : -1;
 }
 
 __device__ __forceinline__ float4 shfl_xyz(const float4& p, int src) {
