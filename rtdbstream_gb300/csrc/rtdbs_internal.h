@@ -25,14 +25,15 @@
 
 namespace rtdbs {
 
-constexpr int kChunkMax = 16384;   // points per grid-update chunk (one-CTA radix sort)
+constexpr int kChunkMax = 16384;   // points per grid-update chunk
 constexpr int kOffBits = 14;       // in-chunk offset bits of a sort word
 constexpr int kKeyBitsMax = 50;    // cell-key bits (key << 14 | offset fits in 64 bits)
 constexpr unsigned long long kKeyMask = (1ull << kKeyBitsMax) - 1ull;
 constexpr unsigned kGenMod = 16383;  // table generations 1..16383 (tag = gen << 50 | key)
 constexpr int kMergeTile = 1024;   // old entries per merge block
 constexpr int kMergeThreads = 256;
-constexpr int kSortThreads = 1024;
+constexpr int kSortRun = 1024;     // words per radix-sort CTA (one per thread)
+constexpr int kMaxRuns = kChunkMax / kSortRun;
 constexpr int kBuildThreads = 512;
 constexpr int kClusterThreads = 256;
 constexpr int kMaxIter = 1 << 20;  // bound on every device-side retry loop

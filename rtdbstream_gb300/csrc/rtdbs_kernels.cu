@@ -6,9 +6,9 @@
 //   chunk step (C <= 16384 new points replacing the points of the same slots)
 //     k_ingest  new points -> ring slots + cell keys; expired points saved
 //               (reference: H2D 2289 + compute_cell_id, src/dbscan/aabb.cu:589-610)
-//     k_sort    one-CTA LSD radix sort of the new and of the expired
-//               (cell key, slot) words (reference: sortByCellIdAndOrder,
-//               src/dbscan/thrust_helper.cu:21-29)
+//     k_sort    LSD radix sort of the new and of the expired (cell key, slot)
+//               words in runs of 1024, one CTA per run (reference:
+//               sortByCellIdAndOrder, src/dbscan/thrust_helper.cu:21-29)
 //     k_decr    exact -1 on the neighbour counts of every survivor within Eps
 //               of an expired point, on the old grid
 //     k_merge   old sorted window minus expired plus new, one pass, merge-path
@@ -308,11 +308,6 @@ __device__ __forceinline__ void flush_stats(const View& v, unsigned rechecks, in
     }
 }
 
-__device__ __forceinline__ float4 shfl_pt(const float4& p, int src) {
-    return make_float4(__shfl_sync(kFull, p.x, src), __shfl_sync(kFull, p.y, src),
-                       __shfl_sync(kFull, p.z, src), __shfl_sync(kFull, p.w, src));
-}
-
 // ------------------------------------------------------------------- kernels
 
 // New points of chunk j -> ring slots [el, el+c): float4 + cell key; the
@@ -363,53 +358,41 @@ __device__ __forceinline__ unsigned block_excl_scan_1024(unsigned val, unsigned*
     return r;
 }
 
-// One-CTA stable LSD radix sort (8-bit digits over the key bits of the sort
-// word) of c <= 16384 words; block 0 sorts the new words, block 1 the
-// expired ones.  Warp-level multisplit: lanes with equal digits are ranked
-// from eight ballots; per-(digit, warp) counters are scanned in digit-major
-// order so the order of equal digits is the item order.
-__global__ void __launch_bounds__(kSortThreads, 1) k_sort(View v, int c, int init) {
-    extern __shared__ unsigned long long sort_smem[];
+// Stable LSD radix sort (8-bit digits over the key bits of the sort word) of
+// the chunk's words in independent runs of kSortRun: block (r, 0) sorts run r
+// of the new words, block (r, 1) run r of the expired ones, one word per
+// thread.  Warp-level multisplit: lanes with equal digits are ranked from
+// eight ballots; per-(digit, warp) counters are scanned in digit-major order
+// so the order of equal digits is the item order.  The merge consumes the
+// sorted runs directly.
+__global__ void __launch_bounds__(kSortRun) k_sort(View v, int c, int init) {
+    __shared__ unsigned long long buf[kSortRun];
+    __shared__ unsigned whist[256 * 32];
     __shared__ unsigned wsum[32];
-    unsigned long long* buf = sort_smem;                                       // kChunkMax words
-    unsigned* whist = reinterpret_cast<unsigned*>(sort_smem + kChunkMax);       // 256 x 32
-    const int which = blockIdx.x;
+    const int which = blockIdx.y;
     if (which == 1 && init) return;
-    const unsigned long long* in = which ? v.xsort : v.nsort;
-    unsigned long long* out = which ? v.xword : v.nword;
+    const int r0 = blockIdx.x * kSortRun;
+    const int len = min(kSortRun, c - r0);
+    if (len <= 0) return;
+    const unsigned long long* in = (which ? v.xsort : v.nsort) + r0;
+    unsigned long long* out = (which ? v.xword : v.nword) + r0;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int ipt = (c + kSortThreads - 1) / kSortThreads;  // 1..16
-    const int wbase = w * 32 * ipt;
     const unsigned lt = lanemask_lt(lane);
-    unsigned long long it[16];
-#pragma unroll
-    for (int r = 0; r < 16; ++r) {
-        const int idx = wbase + r * 32 + lane;
-        it[r] = (r < ipt && idx < c) ? in[idx] : ~0ull;
-    }
+    unsigned long long it = tid < len ? in[tid] : ~0ull;
     for (int pass = 0; pass < v.sort_passes; ++pass) {
         const int shift = kOffBits + 8 * pass;
-        for (int i = tid; i < 256 * 32; i += kSortThreads) whist[i] = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) whist[tid + k * kSortRun] = 0;
         __syncthreads();
-        // Rank of each item among the equal digits of its round (lanes with
-        // the same digit found with eight ballots), kept for the scatter.
-        unsigned info[16];
+        const unsigned d = (unsigned)(it >> shift) & 255u;
+        unsigned peers = kFull;
 #pragma unroll
-        for (int r = 0; r < 16; ++r) {
-            info[r] = 0;
-            if (r < ipt) {
-                const unsigned d = (unsigned)(it[r] >> shift) & 255u;
-                unsigned peers = kFull;
-#pragma unroll
-                for (int bit = 0; bit < 8; ++bit) {
-                    const unsigned bm = __ballot_sync(kFull, (d >> bit) & 1u);
-                    peers &= ((d >> bit) & 1u) ? bm : ~bm;
-                }
-                const unsigned rank = __popc(peers & lt), cnt = __popc(peers);
-                info[r] = rank | (cnt << 6);
-                if (rank == 0) whist[d * 32 + w] += cnt;  // this warp's column only
-            }
+        for (int bit = 0; bit < 8; ++bit) {
+            const unsigned bm = __ballot_sync(kFull, (d >> bit) & 1u);
+            peers &= ((d >> bit) & 1u) ? bm : ~bm;
         }
+        const unsigned rank = __popc(peers & lt);
+        if (rank == 0) whist[d * 32 + w] = __popc(peers);
         __syncthreads();
         unsigned loc[8];
         unsigned sum = 0;
@@ -425,29 +408,11 @@ __global__ void __launch_bounds__(kSortThreads, 1) k_sort(View v, int c, int ini
             pre += loc[k];
         }
         __syncthreads();
-#pragma unroll
-        for (int r = 0; r < 16; ++r) {
-            if (r < ipt) {
-                const unsigned d = (unsigned)(it[r] >> shift) & 255u;
-                const unsigned rank = info[r] & 63u, cnt = info[r] >> 6;
-                const unsigned base = whist[d * 32 + w];
-                __syncwarp();
-                if (rank == 0) whist[d * 32 + w] = base + cnt;
-                __syncwarp();
-                buf[base + rank] = it[r];
-            }
-        }
+        buf[whist[d * 32 + w] + rank] = it;
         __syncthreads();
-#pragma unroll
-        for (int r = 0; r < 16; ++r)
-            if (r < ipt) it[r] = buf[wbase + r * 32 + lane];
-        __syncthreads();
+        it = buf[tid];
     }
-#pragma unroll
-    for (int r = 0; r < 16; ++r) {
-        const int idx = wbase + r * 32 + lane;
-        if (r < ipt && idx < c) out[idx] = it[r];
-    }
+    if (tid < len) out[tid] = it;
 }
 
 // -1 on the count of every surviving neighbour of each expired point (old grid).
@@ -501,13 +466,15 @@ __device__ __forceinline__ int count_words_less(const unsigned long long* words,
 }
 
 // Old sorted window minus the expired slots [el, el+c), merged with the c
-// new entries; tile t of the old window goes to output offset
-// ts - (#expired before ts) + (#new before old[ts]).
+// new entries (held as sorted runs of kSortRun words); tile t of the old
+// window goes to output offset ts - (#expired before ts) + (#new before
+// old[ts]), each count summed over the runs.
 __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, int init) {
     __shared__ unsigned long long tkey[kMergeTile];
     __shared__ int tslot[kMergeTile];
     __shared__ int spre[kMergeTile + 1];
     __shared__ unsigned wsum[32];
+    __shared__ int rn0[kMaxRuns], rn1[kMaxRuns], rx[kMaxRuns];
     const long long b = v.ctl->b;
     const int src = (int)((b - 1) & 1), dst = (int)(b & 1);
     const int n_old = v.ctl->nocc[src];
@@ -537,25 +504,38 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
     unsigned long long* dkey = v.skey[dst];
     float4* dpt = v.spt[dst];
     int* dcnt = v.scnt[dst];
+    const int nruns = (c + kSortRun - 1) / kSortRun;
 
-    int jt0 = 0, jt1 = c, e0 = 0;
-    if (tlen > 0) {
-        const unsigned long long k0 = okey[ts];
-        const int s0 = slot_of(opt[ts]);
-        if (t > 0) jt0 = count_words_less(v.nword, c, el, k0, s0);
-        if (!init) e0 = count_words_less(v.xword, c, el, k0, s0);
-        if (t < ntiles - 1) jt1 = count_words_less(v.nword, c, el, okey[te], slot_of(opt[te]));
+    // Per run: the range of new words that fall in this tile, and the expired
+    // words before it.
+    if (tid < nruns) {
+        const int rb = tid * kSortRun, rl = min(kSortRun, c - rb);
+        int a = 0, z = rl, x = 0;
+        if (tlen > 0) {
+            const unsigned long long k0 = okey[ts];
+            const int s0 = slot_of(opt[ts]);
+            if (t > 0) a = count_words_less(v.nword + rb, rl, el, k0, s0);
+            if (!init) x = count_words_less(v.xword + rb, rl, el, k0, s0);
+            if (t < ntiles - 1) z = count_words_less(v.nword + rb, rl, el, okey[te], slot_of(opt[te]));
+        }
+        rn0[tid] = rb + a;
+        rn1[tid] = rb + z;
+        rx[tid] = x;
+    }
+    // tile -> shared memory
+    for (int i = tid; i < tlen; i += kMergeThreads) {
+        tkey[i] = okey[ts + i];
+        tslot[i] = slot_of(opt[ts + i]);
+    }
+    __syncthreads();
+    int jt0 = 0, e0 = 0;
+    for (int r = 0; r < nruns; ++r) {
+        jt0 += rn0[r] - r * kSortRun;
+        e0 += rx[r];
     }
     const int base = ts - e0 + jt0;
 
-    // tile -> shared memory; survivor prefix in item order
-    for (int i = tid; i < kMergeTile; i += kMergeThreads) {
-        if (i < tlen) {
-            tkey[i] = okey[ts + i];
-            tslot[i] = slot_of(opt[ts + i]);
-        }
-    }
-    __syncthreads();
+    // survivor prefix in item order
     unsigned flags[4];
     unsigned cnt = 0;
 #pragma unroll
@@ -565,7 +545,6 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
         flags[k] = surv ? 1u : 0u;
         cnt += flags[k];
     }
-    // 256-thread exclusive scan
     {
         const int lane = tid & 31, w = tid >> 5;
         unsigned incl = cnt;
@@ -598,11 +577,12 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
     __syncthreads();
 
     // survivors (coalesced, item order i = tid + 256 k)
-    const int m = jt1 - jt0;
     for (int i = tid; i < tlen; i += kMergeThreads) {
         const int s = tslot[i];
         if (!(init || s < el || s >= el + c)) continue;
-        const int lessnew = m > 0 ? count_words_less(v.nword + jt0, m, el, tkey[i], s) : 0;
+        int lessnew = 0;
+        for (int r = 0; r < nruns; ++r)
+            if (rn1[r] > rn0[r]) lessnew += count_words_less(v.nword + rn0[r], rn1[r] - rn0[r], el, tkey[i], s);
         const int o = base + spre[i] + lessnew;
         if (o < 0 || o >= n_new) {
             atomicOr(&v.ctl->err, kErrChunk);
@@ -614,29 +594,35 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
         v.sroot[o] = s;
         v.parent[s] = s;
     }
-    // new entries of this tile
-    for (int q = jt0 + tid; q < jt1; q += kMergeThreads) {
-        const unsigned long long wd = v.nword[q];
-        const unsigned long long key = wd >> kOffBits;
-        const int slot = el + (int)(wd & ((1u << kOffBits) - 1));
-        int lo = 0, hi = tlen;  // old tile entries below (key, slot)
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (tuple_less(tkey[mid], tslot[mid], key, slot))
-                lo = mid + 1;
-            else
-                hi = mid;
+    // new entries of this tile, run by run
+    for (int r = 0; r < nruns; ++r) {
+        for (int q = rn0[r] + tid; q < rn1[r]; q += kMergeThreads) {
+            const unsigned long long wd = v.nword[q];
+            const unsigned long long key = wd >> kOffBits;
+            const int slot = el + (int)(wd & ((1u << kOffBits) - 1));
+            int rank = q - rn0[r];  // new entries of this tile below it, all runs
+            for (int r2 = 0; r2 < nruns; ++r2)
+                if (r2 != r && rn1[r2] > rn0[r2])
+                    rank += count_words_less(v.nword + rn0[r2], rn1[r2] - rn0[r2], el, key, slot);
+            int lo = 0, hi = tlen;  // old tile entries below (key, slot)
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (tuple_less(tkey[mid], tslot[mid], key, slot))
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            const int o = base + rank + spre[lo];
+            if (o < 0 || o >= n_new || slot < 0 || slot >= v.W) {
+                atomicOr(&v.ctl->err, kErrChunk);
+                continue;
+            }
+            dkey[o] = key;
+            dpt[o] = v.ring[slot];
+            dcnt[o] = 0;
+            v.sroot[o] = slot;
+            v.parent[slot] = slot;
         }
-        const int o = base + (q - jt0) + spre[lo];
-        if (o < 0 || o >= n_new || slot < 0 || slot >= v.W) {
-            atomicOr(&v.ctl->err, kErrChunk);
-            continue;
-        }
-        dkey[o] = key;
-        dpt[o] = v.ring[slot];
-        dcnt[o] = 0;
-        v.sroot[o] = slot;
-        v.parent[slot] = slot;
     }
 }
 
@@ -757,9 +743,11 @@ __global__ void __launch_bounds__(256) k_incr(View v, int j, int c, int init) {
 template <int MODE, int DIM>
 __global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
     __shared__ int home_root[kClusterThreads / 32][32];
+    __shared__ float4 home_pt[kClusterThreads / 32][32];
     __shared__ int rstart[kClusterThreads / 32][9], rpre[kClusterThreads / 32][10];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     volatile int* rh = home_root[wib];
+    const float4* hpt = home_pt[wib];
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const long long b = v.ctl->b;
@@ -791,7 +779,9 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
         }
         const unsigned hmask = __ballot_sync(kFull, hcore);
         if (!hmask) continue;
+        __syncwarp();
         if (hcore) rh[lane] = hint[start + lane];
+        home_pt[wib][lane] = h;
         const int hmin = start + __ffs(hmask) - 1;
         int rs, re;
         row_ranges<DIM>(v, T, gen, skey[start], lane, rs, re);
@@ -811,13 +801,14 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
                 }
             }
             if (!__any_sync(kFull, qc)) continue;
+            // Pairs whose hints already agree are in one set: no test, no link.
             unsigned adj = 0;
             unsigned mm = hmask;
             while (mm) {
                 const int hi = __ffs(mm) - 1;
                 mm &= mm - 1;
-                const float4 hp = shfl_pt(h, hi);
-                if (qc && pos > start + hi && is_nbr<MODE, DIM>(v, hp, q, rechecks)) adj |= 1u << hi;
+                if (qc && pos > start + hi && qh != rh[hi] && is_nbr<MODE, DIM>(v, hpt[hi], q, rechecks))
+                    adj |= 1u << hi;
             }
             if (adj) {
                 int rq = uf_find(parent, qh);
@@ -827,7 +818,7 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
                     const int ra = rh[hi];
                     if (ra != rq) {
                         rq = uf_link(parent, ra, rq, err);
-                        rh[hi] = rq;
+                        rh[hi] = rq;  // an ancestor of both points (benign race)
                     }
                 }
                 if (rq != qh) hint[pos] = rq;
@@ -849,17 +840,14 @@ __global__ void k_flatten(View v) {
         v.sroot[i] = scnt[i] >= v.min_pts ? uf_find(v.parent, v.sroot[i]) : -1;
 }
 
-__device__ __forceinline__ float4 shfl_xyz(const float4& p, int src) {
-    return make_float4(__shfl_sync(kFull, p.x, src), __shfl_sync(kFull, p.y, src),
-                       __shfl_sync(kFull, p.z, src), 0.f);
-}
-
 // Labels and ids by slot: core -> 0 and its root; non-core -> 1 and the
 // minimum root over adjacent cores, or 2 and its own slot.
 template <int MODE, int DIM>
 __global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advance) {
     __shared__ int rstart[kClusterThreads / 32][9], rpre[kClusterThreads / 32][10];
+    __shared__ float4 home_pt[kClusterThreads / 32][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const float4* hpt = home_pt[wib];
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const long long b = v.ctl->b;
@@ -890,6 +878,8 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advanc
         }
         const unsigned nmask = __ballot_sync(kFull, hv && hr < 0);
         if (!nmask) continue;
+        __syncwarp();
+        home_pt[wib][lane] = h;
         int rs, re;
         row_ranges<DIM>(v, T, gen, skey[start], lane, rs, re);
         const int total = candidate_stream<DIM>(rs, re, 0, lane, rstart[wib], rpre[wib]);
@@ -908,8 +898,7 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advanc
             while (mm) {
                 const int hi = __ffs(mm) - 1;
                 mm &= mm - 1;
-                const float4 hp = shfl_xyz(h, hi);
-                const int val = (qr >= 0 && is_nbr<MODE, DIM>(v, hp, q, rechecks)) ? qr : INT_MAX;
+                const int val = (qr >= 0 && is_nbr<MODE, DIM>(v, hpt[hi], q, rechecks)) ? qr : INT_MAX;
                 const int mn = (int)__reduce_min_sync(kFull, (unsigned)val);
                 if (lane == hi) best = min(best, mn);
             }
@@ -952,7 +941,6 @@ int g_num_sms = 0;
         }                                                                        \
     } while (0)
 
-static constexpr size_t kSortSmem = sizeof(unsigned long long) * kChunkMax + sizeof(unsigned) * 256 * 32;
 
 cudaError_t configure_kernels() {
     int dev = 0;
@@ -960,7 +948,7 @@ cudaError_t configure_kernels() {
     if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSortSmem);
+    return cudaSuccess;
 }
 
 cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, int init,
@@ -971,7 +959,7 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
             k_ingest<<<(c + 255) / 256, 256, 0, s>>>(v, j, c, init, stg_off);
             break;
         case kPhaseSort:
-            k_sort<<<init ? 1 : 2, kSortThreads, kSortSmem, s>>>(v, c, init);
+            k_sort<<<dim3((c + kSortRun - 1) / kSortRun, init ? 1 : 2), kSortRun, 0, s>>>(v, c, init);
             break;
         case kPhaseDecrement:
             if (!init) RTDBS_DISPATCH(precision, v.dim, k_decr, warp_blocks, 256, s, v, j, c);
