@@ -475,6 +475,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
     __shared__ int spre[kMergeTile + 1];
     __shared__ unsigned wsum[32];
     __shared__ int rn0[kMaxRuns], rn1[kMaxRuns], rx[kMaxRuns];
+    __shared__ unsigned long long tnew[kMergeNewCap];
     const long long b = v.ctl->b;
     const int src = (int)((b - 1) & 1), dst = (int)(b & 1);
     const int n_old = v.ctl->nocc[src];
@@ -576,13 +577,37 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
     }
     __syncthreads();
 
+    // The tile's new words from all runs, merged in shared memory when they fit.
+    int m = 0;
+    for (int r = 0; r < nruns; ++r) m += rn1[r] - rn0[r];
+    const bool staged = m <= kMergeNewCap;
+    if (staged) {
+        for (int r = 0; r < nruns; ++r) {
+            for (int q = rn0[r] + tid; q < rn1[r]; q += kMergeThreads) {
+                const unsigned long long wd = v.nword[q];
+                const unsigned long long key = wd >> kOffBits;
+                const int slot = el + (int)(wd & ((1u << kOffBits) - 1));
+                int rank = q - rn0[r];
+                for (int r2 = 0; r2 < nruns; ++r2)
+                    if (r2 != r && rn1[r2] > rn0[r2])
+                        rank += count_words_less(v.nword + rn0[r2], rn1[r2] - rn0[r2], el, key, slot);
+                tnew[rank] = wd;
+            }
+        }
+        __syncthreads();
+    }
+
     // survivors (coalesced, item order i = tid + 256 k)
     for (int i = tid; i < tlen; i += kMergeThreads) {
         const int s = tslot[i];
         if (!(init || s < el || s >= el + c)) continue;
         int lessnew = 0;
-        for (int r = 0; r < nruns; ++r)
-            if (rn1[r] > rn0[r]) lessnew += count_words_less(v.nword + rn0[r], rn1[r] - rn0[r], el, tkey[i], s);
+        if (staged) {
+            if (m > 0) lessnew = count_words_less(tnew, m, el, tkey[i], s);
+        } else {
+            for (int r = 0; r < nruns; ++r)
+                if (rn1[r] > rn0[r]) lessnew += count_words_less(v.nword + rn0[r], rn1[r] - rn0[r], el, tkey[i], s);
+        }
         const int o = base + spre[i] + lessnew;
         if (o < 0 || o >= n_new) {
             atomicOr(&v.ctl->err, kErrChunk);
@@ -594,16 +619,21 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
         v.sroot[o] = s;
         v.parent[s] = s;
     }
-    // new entries of this tile, run by run
-    for (int r = 0; r < nruns; ++r) {
-        for (int q = rn0[r] + tid; q < rn1[r]; q += kMergeThreads) {
-            const unsigned long long wd = v.nword[q];
+    // new entries of this tile (merged order from shared memory, or run by run)
+    const int nq = staged ? m : 0;
+    for (int r = staged ? nruns : 0; r <= nruns; ++r) {
+        const bool from_smem = r == nruns;
+        if (from_smem && !staged) break;
+        const int q0 = from_smem ? 0 : rn0[r], q1 = from_smem ? nq : rn1[r];
+        for (int q = q0 + tid; q < q1; q += kMergeThreads) {
+            const unsigned long long wd = from_smem ? tnew[q] : v.nword[q];
             const unsigned long long key = wd >> kOffBits;
             const int slot = el + (int)(wd & ((1u << kOffBits) - 1));
-            int rank = q - rn0[r];  // new entries of this tile below it, all runs
-            for (int r2 = 0; r2 < nruns; ++r2)
-                if (r2 != r && rn1[r2] > rn0[r2])
-                    rank += count_words_less(v.nword + rn0[r2], rn1[r2] - rn0[r2], el, key, slot);
+            int rank = q - q0;  // new entries of this tile below it, all runs
+            if (!from_smem)
+                for (int r2 = 0; r2 < nruns; ++r2)
+                    if (r2 != r && rn1[r2] > rn0[r2])
+                        rank += count_words_less(v.nword + rn0[r2], rn1[r2] - rn0[r2], el, key, slot);
             int lo = 0, hi = tlen;  // old tile entries below (key, slot)
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
