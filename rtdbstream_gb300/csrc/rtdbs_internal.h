@@ -37,7 +37,6 @@ constexpr int kSortRun = 1024;     // words per radix-sort CTA (one per thread)
 constexpr int kMaxRuns = kChunkMax / kSortRun;
 constexpr int kBuildThreads = 512;
 constexpr int kClusterThreads = 256;
-constexpr int kStage = 128;        // core candidates staged per warp in the union
 constexpr int kMaxIter = 1 << 20;  // bound on every device-side retry loop
 
 // Bits of Ctl::err.

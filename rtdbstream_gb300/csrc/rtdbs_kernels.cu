@@ -775,15 +775,9 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
     __shared__ int home_root[kClusterThreads / 32][32];
     __shared__ float4 home_pt[kClusterThreads / 32][32];
     __shared__ int rstart[kClusterThreads / 32][9], rpre[kClusterThreads / 32][10];
-    __shared__ float4 stage_pt[kClusterThreads / 32][kStage];
-    __shared__ int stage_pos[kClusterThreads / 32][kStage];
-    __shared__ int stage_hint[kClusterThreads / 32][kStage];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     volatile int* rh = home_root[wib];
     const float4* hpt = home_pt[wib];
-    float4* cpt = stage_pt[wib];
-    int* cpos = stage_pos[wib];
-    int* chint = stage_hint[wib];
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const long long b = v.ctl->b;
@@ -822,71 +816,42 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
         int rs, re;
         row_ranges<DIM>(v, T, gen, skey[start], lane, rs, re);
         const int total = candidate_stream<DIM>(rs, re, hmin + 1, lane, rstart[wib], rpre[wib]);
-        const int hfirst = __ffs(hmask) - 1;
-        int r = 0, consumed = 0;
-        while (consumed < total) {
-            // Stage up to kStage core candidates, compacted (loads stay in full
-            // 32-wide chunks of the candidate stream).
-            int n = 0;
-            while (consumed < total && n <= kStage - 32) {
-                const int idx = consumed + lane;
-                bool qc = false;
-                int pos = 0, qh = 0;
-                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (idx < total) {
-                    pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
+        int r = 0;
+        for (int base = 0; base < total; base += 32) {
+            const int idx = base + lane;
+            int pos = 0, qh = 0;
+            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+            bool qc = false;
+            if (idx < total) {
+                pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
+                qc = scnt[pos] >= v.min_pts;
+                if (qc) {
                     q = spt[pos];
                     qh = hint[pos];
-                    qc = scnt[pos] >= v.min_pts;
                 }
-                const unsigned m = __ballot_sync(kFull, qc);
-                if (qc) {
-                    const int o = n + __popc(m & lanemask_lt(lane));
-                    cpt[o] = q;
-                    cpos[o] = pos;
-                    chint[o] = qh;
-                }
-                n += __popc(m);
-                consumed += 32;
             }
-            __syncwarp();
-            for (int c0 = 0; c0 < n; c0 += 32) {
-                const int ci = c0 + lane;
-                const bool cv = ci < n;
-                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-                int pos = 0, qh = -1;
-                if (cv) {
-                    q = cpt[ci];
-                    pos = cpos[ci];
-                    qh = chint[ci];
-                }
-                // Homes sharing one root and candidates already hinted to it:
-                // the whole chunk is in one set.
-                const int r0 = rh[hfirst];
-                if (__all_sync(kFull, (!hcore || rh[lane] == r0) && (!cv || qh == r0))) continue;
-                // Pairs whose hints already agree are in one set: no test, no link.
-                unsigned adj = 0;
-                unsigned mm = hmask;
-                while (mm) {
-                    const int hi = __ffs(mm) - 1;
-                    mm &= mm - 1;
-                    if (cv && pos > start + hi && qh != rh[hi] && is_nbr<MODE, DIM>(v, hpt[hi], q, rechecks))
-                        adj |= 1u << hi;
-                }
-                if (adj) {
-                    int rq = uf_find(parent, qh);
-                    while (adj) {
-                        const int hi = __ffs(adj) - 1;
-                        adj &= adj - 1;
-                        const int ra = rh[hi];
-                        if (ra != rq) {
-                            rq = uf_link(parent, ra, rq, err);
-                            rh[hi] = rq;  // an ancestor of both points (benign race)
-                        }
+            if (!__any_sync(kFull, qc)) continue;
+            // Pairs whose hints already agree are in one set: no test, no link.
+            unsigned adj = 0;
+            unsigned mm = hmask;
+            while (mm) {
+                const int hi = __ffs(mm) - 1;
+                mm &= mm - 1;
+                if (qc && pos > start + hi && qh != rh[hi] && is_nbr<MODE, DIM>(v, hpt[hi], q, rechecks))
+                    adj |= 1u << hi;
+            }
+            if (adj) {
+                int rq = uf_find(parent, qh);
+                while (adj) {
+                    const int hi = __ffs(adj) - 1;
+                    adj &= adj - 1;
+                    const int ra = rh[hi];
+                    if (ra != rq) {
+                        rq = uf_link(parent, ra, rq, err);
+                        rh[hi] = rq;  // an ancestor of both points (benign race)
                     }
-                    if (rq != qh) hint[pos] = rq;
                 }
-                __syncwarp();
+                if (rq != qh) hint[pos] = rq;
             }
             __syncwarp();
         }
@@ -911,12 +876,8 @@ template <int MODE, int DIM>
 __global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advance) {
     __shared__ int rstart[kClusterThreads / 32][9], rpre[kClusterThreads / 32][10];
     __shared__ float4 home_pt[kClusterThreads / 32][32];
-    __shared__ float4 stage_pt[kClusterThreads / 32][kStage];
-    __shared__ int stage_root[kClusterThreads / 32][kStage];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const float4* hpt = home_pt[wib];
-    float4* cpt = stage_pt[wib];
-    int* croot = stage_root[wib];
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const long long b = v.ctl->b;
@@ -952,48 +913,25 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advanc
         int rs, re;
         row_ranges<DIM>(v, T, gen, skey[start], lane, rs, re);
         const int total = candidate_stream<DIM>(rs, re, 0, lane, rstart[wib], rpre[wib]);
-        int best = INT_MAX, r = 0, consumed = 0;
-        while (consumed < total) {
-            // Stage up to kStage core candidates (roots), compacted.
-            int n = 0;
-            while (consumed < total && n <= kStage - 32) {
-                const int idx = consumed + lane;
-                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-                int qr = -1;
-                if (idx < total) {
-                    const int pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
-                    q = spt[pos];
-                    qr = sroot[pos];
-                }
-                const unsigned m = __ballot_sync(kFull, qr >= 0);
-                if (qr >= 0) {
-                    const int o = n + __popc(m & lanemask_lt(lane));
-                    cpt[o] = q;
-                    croot[o] = qr;
-                }
-                n += __popc(m);
-                consumed += 32;
+        int best = INT_MAX, r = 0;
+        for (int base = 0; base < total; base += 32) {
+            const int idx = base + lane;
+            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+            int qr = -1;
+            if (idx < total) {
+                const int pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
+                qr = sroot[pos];
+                if (qr >= 0) q = spt[pos];
             }
-            __syncwarp();
-            for (int c0 = 0; c0 < n; c0 += 32) {
-                const int ci = c0 + lane;
-                const bool cv = ci < n;
-                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-                int qr = INT_MAX;
-                if (cv) {
-                    q = cpt[ci];
-                    qr = croot[ci];
-                }
-                unsigned mm = nmask;
-                while (mm) {
-                    const int hi = __ffs(mm) - 1;
-                    mm &= mm - 1;
-                    const int val = (cv && is_nbr<MODE, DIM>(v, hpt[hi], q, rechecks)) ? qr : INT_MAX;
-                    const int mn = (int)__reduce_min_sync(kFull, (unsigned)val);
-                    if (lane == hi) best = min(best, mn);
-                }
+            if (!__any_sync(kFull, qr >= 0)) continue;
+            unsigned mm = nmask;
+            while (mm) {
+                const int hi = __ffs(mm) - 1;
+                mm &= mm - 1;
+                const int val = (qr >= 0 && is_nbr<MODE, DIM>(v, hpt[hi], q, rechecks)) ? qr : INT_MAX;
+                const int mn = (int)__reduce_min_sync(kFull, (unsigned)val);
+                if (lane == hi) best = min(best, mn);
             }
-            __syncwarp();
         }
         if (hv && hr < 0) {
             if (best != INT_MAX) {
