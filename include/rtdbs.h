@@ -177,6 +177,30 @@ RTDBS_API int rtdbs_device_outputs(rtdbs_engine* engine, int32_t** d_label, int3
 
 RTDBS_API int rtdbs_get_stats(rtdbs_engine* engine, rtdbs_stats* stats);
 
+/* Largest window rtdbs_cluster_window_noalloc accepts. */
+#define RTDBS_NOALLOC_MAX_POINTS 16384
+
+/* Clusters one window of n <= RTDBS_NOALLOC_MAX_POINTS points without
+ * allocating any memory.  No counterpart in the reference: it exists for
+ * callers that cannot call cudaMalloc (a host process that keeps the GPU's
+ * memory in its own pool and forbids raw allocations by plug-ins, or a caller
+ * on a latency path that cannot take cudaMalloc's implicit synchronisation).
+ * Inputs and outputs are device memory owned by the caller: d_points[n][dim],
+ * d_label[n], d_cluster_id[n] (index = the point's position in d_points, with
+ * the same labels and ids as rtdbs_load_window + rtdbs_cluster on a window of
+ * n slots).  Working memory is one static device array of about 3.4 MB,
+ * part of the library: every GPU that loads the library holds it until the
+ * process exits.  The first call on a device looks up that array's device
+ * address (with that device current); make the first call before any stream
+ * capture.  All calls share the array: calls whose work overlaps on a GPU
+ * race and corrupt each other's results, so serialise them.  Runs on
+ * cuda_stream (a cudaStream_t, NULL = default stream) and returns after the
+ * stream has finished.  Returns RTDBS_ERR_INVALID for n above the limit or
+ * bad arguments, RTDBS_ERR_DEVICE if a device-side bound was hit. */
+RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int32_t n, int32_t dim, double eps,
+                                           int32_t min_pts, int32_t precision, int32_t* d_label,
+                                           int32_t* d_cluster_id, void* cuda_stream);
+
 /* rtdbs_slide_async with every kernel launched directly and bracketed by CUDA
  * events; synchronous.  Results are identical to an ordinary slide. */
 RTDBS_API int rtdbs_slide_profiled(rtdbs_engine* engine, const float* d_new_points,

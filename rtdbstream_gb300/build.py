@@ -29,7 +29,8 @@ def nvcc() -> str:
 
 
 def sources() -> list[str]:
-    return [os.path.join(CSRC, "rtdbs_kernels.cu"), os.path.join(CSRC, "rtdbs_engine.cpp")]
+    return [os.path.join(CSRC, "rtdbs_kernels.cu"), os.path.join(CSRC, "rtdbs_engine.cpp"),
+            os.path.join(CSRC, "rtdbs_noalloc.cu")]
 
 
 def headers() -> list[str]:

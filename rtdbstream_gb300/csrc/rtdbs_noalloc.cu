@@ -1,0 +1,244 @@
+// rtdbs_noalloc.cu -- clustering of one window of points with no device
+// memory allocation (rtdbs_cluster_window_noalloc in include/rtdbs.h).
+//
+// Some callers cannot call cudaMalloc: a host process (a database engine or
+// stream processor, say) that reserves the GPU's memory for its own pool at
+// start-up and forbids raw allocations by plug-ins, or a caller on a latency
+// path where cudaMalloc's implicit device synchronisation is unacceptable.
+// For them this entry point runs the same kernels as rtdbs_load_window +
+// rtdbs_cluster on at most RTDBS_NOALLOC_MAX_POINTS points, with all of its
+// working memory in one file-scope __device__ array (below).  That array is
+// part of the library image: every GPU that loads the library holds it until
+// the process exits.  The caller passes the input points and the two output
+// arrays (device memory); nothing else is allocated, by us or by a library.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include <cuda_runtime.h>
+
+#include "rtdbs.h"
+#include "rtdbs_internal.h"
+
+namespace {
+
+using rtdbs::Ctl;
+using rtdbs::View;
+
+constexpr int kMaxPoints = RTDBS_NOALLOC_MAX_POINTS;
+static_assert(kMaxPoints <= rtdbs::kChunkMax, "one grid-update chunk must hold the window");
+constexpr unsigned long long kTableSlots = 32768;  // power of two >= 2 * kMaxPoints
+static_assert(kTableSlots >= 2ull * kMaxPoints, "table capacity");
+constexpr int kMaxItems = kMaxPoints + kMaxPoints / 32 + 64;
+
+constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// Byte offsets of every buffer inside the scratch array.
+constexpr size_t kOffRing = 0;
+constexpr size_t kOffKslot = kOffRing + align256(sizeof(float4) * kMaxPoints);
+constexpr size_t kOffSkey0 = kOffKslot + align256(sizeof(unsigned long long) * kMaxPoints);
+constexpr size_t kOffSkey1 = kOffSkey0 + align256(sizeof(unsigned long long) * kMaxPoints);
+constexpr size_t kOffSpt0 = kOffSkey1 + align256(sizeof(unsigned long long) * kMaxPoints);
+constexpr size_t kOffSpt1 = kOffSpt0 + align256(sizeof(float4) * kMaxPoints);
+constexpr size_t kOffScnt0 = kOffSpt1 + align256(sizeof(float4) * kMaxPoints);
+constexpr size_t kOffScnt1 = kOffScnt0 + align256(sizeof(int) * kMaxPoints);
+constexpr size_t kOffTable0 = kOffScnt1 + align256(sizeof(int) * kMaxPoints);
+constexpr size_t kOffTable1 = kOffTable0 + align256(sizeof(ulonglong2) * kTableSlots);
+constexpr size_t kOffItems = kOffTable1 + align256(sizeof(ulonglong2) * kTableSlots);
+constexpr size_t kOffParent = kOffItems + align256(sizeof(int2) * kMaxItems);
+constexpr size_t kOffSroot = kOffParent + align256(sizeof(int) * kMaxPoints);
+constexpr size_t kOffNsort = kOffSroot + align256(sizeof(int) * kMaxPoints);
+constexpr size_t kOffXsort = kOffNsort + align256(sizeof(unsigned long long) * kMaxPoints);
+constexpr size_t kOffNword = kOffXsort + align256(sizeof(unsigned long long) * kMaxPoints);
+constexpr size_t kOffXword = kOffNword + align256(sizeof(unsigned long long) * kMaxPoints);
+constexpr size_t kOffXpt = kOffXword + align256(sizeof(unsigned long long) * kMaxPoints);
+constexpr size_t kOffBox = kOffXpt + align256(sizeof(float4) * kMaxPoints);
+constexpr size_t kOffCtl = kOffBox + align256(sizeof(float) * 6);
+constexpr size_t kScratchBytes = kOffCtl + align256(sizeof(Ctl));  // about 3.4 MB
+
+// The working memory.  In host code this name is only a host-side stand-in
+// for the device array: its device address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mutex;
+unsigned char* g_scratch_ptr[kMaxDevices] = {nullptr};
+
+// Per-axis finite minimum and maximum of the points, written to box[0..5]
+// (min x, y, z, max x, y, z); one block.
+__global__ void k_noalloc_bbox(const float* pts, int n, int dim, float* box) {
+    __shared__ float lo[3][32], hi[3][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int a = 0; a < 3; ++a) {
+        float l = INFINITY, h = -INFINITY;
+        if (a < dim) {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                const float x = pts[(size_t)i * dim + a];
+                if (isfinite(x)) {
+                    l = fminf(l, x);
+                    h = fmaxf(h, x);
+                }
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            l = fminf(l, __shfl_xor_sync(0xffffffffu, l, o));
+            h = fmaxf(h, __shfl_xor_sync(0xffffffffu, h, o));
+        }
+        if (lane == 0) {
+            lo[a][w] = l;
+            hi[a][w] = h;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int a = threadIdx.x;
+        float l = INFINITY, h = -INFINITY;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+            l = fminf(l, lo[a][k]);
+            h = fmaxf(h, hi[a][k]);
+        }
+        if (!(l <= h)) l = h = 0.0f;  // no finite coordinate on this axis
+        box[a] = l;
+        box[3 + a] = h;
+    }
+}
+
+// Device address of g_scratch on the current device (set up on the first
+// call per device, with that device current).
+int scratch_for_current_device(unsigned char** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+        return RTDBS_ERR_NO_DEVICE;
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+        if (e != cudaSuccess || !p) return RTDBS_ERR_CUDA;
+        g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = g_scratch_ptr[dev];
+    return RTDBS_OK;
+}
+
+}  // namespace
+
+extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int32_t n, int32_t dim,
+                                                      double eps, int32_t min_pts, int32_t precision,
+                                                      int32_t* d_label, int32_t* d_cluster_id,
+                                                      void* cuda_stream) {
+    if (!d_points || !d_label || !d_cluster_id) return RTDBS_ERR_INVALID;
+    if (n < 0 || n > kMaxPoints) return RTDBS_ERR_INVALID;  // beyond the scratch array
+    if (dim < 1 || dim > 3) return RTDBS_ERR_INVALID;
+    if (!(eps > 0.0) || !std::isfinite(eps)) return RTDBS_ERR_INVALID;
+    if (precision != RTDBS_PREC_FP64 && precision != RTDBS_PREC_FP32) return RTDBS_ERR_INVALID;
+    if (n == 0) return RTDBS_OK;
+    unsigned char* base = nullptr;
+    int rc = scratch_for_current_device(&base);
+    if (rc != RTDBS_OK) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+
+#define NOALLOC_TRY(expr)                                                      \
+    do {                                                                       \
+        const cudaError_t _e = (expr);                                         \
+        if (_e != cudaSuccess) return RTDBS_ERR_CUDA;                          \
+    } while (0)
+
+    // Every call reuses the array, which still holds the previous call's
+    // data: the cell tables (generation tags) and the control block must
+    // start at zero; everything else is rewritten before it is read.
+    NOALLOC_TRY(cudaMemsetAsync(base + kOffTable0, 0, sizeof(ulonglong2) * kTableSlots * 2, s));
+    NOALLOC_TRY(cudaMemsetAsync(base + kOffCtl, 0, sizeof(Ctl), s));
+
+    // Bounding box -> grid geometry (same rules as an engine without a box).
+    float* d_box = reinterpret_cast<float*>(base + kOffBox);
+    k_noalloc_bbox<<<1, 1024, 0, s>>>(d_points, n, dim, d_box);
+    NOALLOC_TRY(cudaGetLastError());
+    float box[6];
+    NOALLOC_TRY(cudaMemcpyAsync(box, d_box, sizeof(box), cudaMemcpyDeviceToHost, s));
+    NOALLOC_TRY(cudaStreamSynchronize(s));
+
+    View v;
+    std::memset(&v, 0, sizeof(v));
+    v.dim = dim;
+    v.W = n;
+    v.S = n;
+    v.units = 1;
+    v.min_pts = min_pts;
+    v.chunk = n;
+    const double E = eps * eps, m = 1.0 / 1048576.0;
+    float flo = (float)(E * (1.0 - m)), fhi = (float)(E * (1.0 + m));
+    if ((double)flo > E * (1.0 - m)) flo = std::nextafter(flo, 0.0f);
+    if ((double)fhi < E * (1.0 + m)) fhi = std::nextafter(fhi, INFINITY);
+    v.lo = flo;
+    v.hi = fhi;
+    v.E = E;
+    v.filter_ok = (E >= std::ldexp(1.0, -100) && E <= std::ldexp(1.0, 100)) ? 1 : 0;
+    const float r = (float)eps;
+    v.r2f = r * r;
+    double L = eps * (1.0 + 1.0 / 4096.0);
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int a = 0; a < dim; ++a) {
+        const double mg = std::max(0.25 * ((double)box[3 + a] - box[a]), 4.0 * L);
+        lo[a] = box[a] - mg;
+        hi[a] = box[3 + a] + mg;
+    }
+    long long ext[3] = {1, 1, 1};
+    int bits[3] = {0, 0, 0};
+    for (int guard = 0; guard < 4096; ++guard) {
+        int total = 0;
+        for (int a = 0; a < dim; ++a) {
+            const double cells = std::floor((hi[a] - lo[a]) / L) + 1.0;
+            ext[a] = cells < 4.0e15 ? (long long)cells : (long long)4.0e15;
+            bits[a] = 0;
+            while (bits[a] < 62 && (1ll << bits[a]) < ext[a]) ++bits[a];
+            total += bits[a];
+        }
+        if (total <= rtdbs::kKeyBitsMax) break;
+        L *= 2.0;
+    }
+    for (int a = 0; a < 3; ++a) {
+        v.origin[a] = lo[a];
+        v.ext[a] = ext[a];
+    }
+    v.shift[2] = 0;
+    v.shift[1] = bits[2];
+    v.shift[0] = bits[1] + bits[2];
+    v.inv_cell = 1.0 / L;
+    v.key_bits = bits[0] + bits[1] + bits[2];
+    v.sort_passes = (v.key_bits + 7) / 8;
+    v.pbits = 15;
+    v.pmask = (unsigned)(kTableSlots - 1);
+    v.max_items = kMaxItems;
+
+    v.ring = reinterpret_cast<float4*>(base + kOffRing);
+    v.kslot = reinterpret_cast<unsigned long long*>(base + kOffKslot);
+    v.skey[0] = reinterpret_cast<unsigned long long*>(base + kOffSkey0);
+    v.skey[1] = reinterpret_cast<unsigned long long*>(base + kOffSkey1);
+    v.spt[0] = reinterpret_cast<float4*>(base + kOffSpt0);
+    v.spt[1] = reinterpret_cast<float4*>(base + kOffSpt1);
+    v.scnt[0] = reinterpret_cast<int*>(base + kOffScnt0);
+    v.scnt[1] = reinterpret_cast<int*>(base + kOffScnt1);
+    v.table[0] = reinterpret_cast<ulonglong2*>(base + kOffTable0);
+    v.table[1] = reinterpret_cast<ulonglong2*>(base + kOffTable1);
+    v.items = reinterpret_cast<int2*>(base + kOffItems);
+    v.parent = reinterpret_cast<int*>(base + kOffParent);
+    v.sroot = reinterpret_cast<int*>(base + kOffSroot);
+    v.label = d_label;
+    v.cid = d_cluster_id;
+    v.nsort = reinterpret_cast<unsigned long long*>(base + kOffNsort);
+    v.xsort = reinterpret_cast<unsigned long long*>(base + kOffXsort);
+    v.nword = reinterpret_cast<unsigned long long*>(base + kOffNword);
+    v.xword = reinterpret_cast<unsigned long long*>(base + kOffXword);
+    v.xpt = reinterpret_cast<float4*>(base + kOffXpt);
+    v.staging = d_points;  // the caller's points are read in place
+    v.ctl = reinterpret_cast<Ctl*>(base + kOffCtl);
+
+    NOALLOC_TRY(rtdbs::launch_chunk_step(v, precision, 0, n, 1, 0, s));
+    NOALLOC_TRY(rtdbs::launch_cluster(v, precision, 0, s));
+    int err = 0;
+    NOALLOC_TRY(cudaMemcpyAsync(&err, &v.ctl->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NOALLOC_TRY(cudaStreamSynchronize(s));
+#undef NOALLOC_TRY
+    return err ? RTDBS_ERR_DEVICE : RTDBS_OK;
+}

@@ -31,7 +31,7 @@ EXPORTED_SYMBOLS = (
     "rtdbs_abi_version", "rtdbs_status_string", "rtdbs_last_error", "rtdbs_params_init",
     "rtdbs_create", "rtdbs_destroy", "rtdbs_load_window", "rtdbs_slide", "rtdbs_slide_async",
     "rtdbs_sync", "rtdbs_cluster", "rtdbs_get_counts", "rtdbs_device_outputs", "rtdbs_get_stats",
-    "rtdbs_slide_profiled",
+    "rtdbs_slide_profiled", "rtdbs_cluster_window_noalloc",
 )
 
 
