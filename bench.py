@@ -227,12 +227,13 @@ def measured_peak() -> tuple:
 
 
 def ncu_traffic(phase: str):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary (profiles/ncu_traffic.json), or None."""
+    """DRAM bytes per launch of the dominant kernel at W = 1M from the
+    committed ncu summary (profiles/ncu_traffic.json, a W = 250k capture
+    scaled by 4), or None."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get(phase)
+            return json.load(f).get(f"k_{phase}")
     except (OSError, ValueError):
         return None
 
