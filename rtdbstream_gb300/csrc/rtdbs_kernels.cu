@@ -763,137 +763,99 @@ __global__ void __launch_bounds__(256) k_incr(View v, int j, int c, int init) {
 }
 
 // Union of every core-core neighbour pair, each unordered pair once (the
-// candidate's sorted position is above the home point's).  One lane per home
-// point: a warp owns 32 consecutive sorted positions, looks up the neighbour
-// rows of the (few) cells among them together, and then every lane walks its
-// own cell's rows with a private cursor, one candidate per iteration, keeping
-// its home's root in a register.  Finds start from per-position root hints
-// (coalesced with the candidate loads); a pair whose hints already agree is
-// in one set and costs no test and no link.
+// candidate's sorted position is above the home point's).  A candidate's
+// root is found once per candidate chunk and compared with cached roots of
+// the home points (shared memory, per warp); a link is attempted only where
+// the two differ, so same-set pairs cost no memory traffic.  Finds start
+// from per-position root hints.  Each warp walks
+// a contiguous range of work items (neighbouring cells), so candidate loads
+// reuse L1.
 template <int MODE, int DIM>
-__global__ void __launch_bounds__(kClusterThreads, 4) k_union(View v) {
-    constexpr int kRows = DIM == 1 ? 1 : (DIM == 2 ? 3 : 9);
-    constexpr int kWarps = kClusterThreads / 32;
-    __shared__ int2 cell_rows[kWarps][32][kRows];
-    __shared__ unsigned long long cell_key[kWarps][32];
+__global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
+    __shared__ int home_root[kClusterThreads / 32][32];
+    __shared__ float4 home_pt[kClusterThreads / 32][32];
+    __shared__ int rstart[kClusterThreads / 32][9], rpre[kClusterThreads / 32][10];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    volatile int* rh = home_root[wib];
+    const float4* hpt = home_pt[wib];
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const long long b = v.ctl->b;
     const int cur = (int)(b & 1);
     const unsigned gen = gen_of_build(b);
-    const int n = v.ctl->nocc[cur];
+    const int nitems = min(v.ctl->nitems, v.max_items);
+    const int per = (nitems + nw - 1) / nw;
+    const int it0 = min(gw * per, nitems), it1 = min(it0 + per, nitems);
     const float4* spt = v.spt[cur];
     const int* scnt = v.scnt[cur];
     const unsigned long long* skey = v.skey[cur];
     const ulonglong2* T = v.table[cur];
     int* parent = v.parent;
     // Root hints by sorted position (an ancestor of the point; the merge sets
-    // each to the point's own slot), refreshed as roots are found.
+    // each to the point's own slot): coalesced with the candidate loads, and
+    // refreshed as roots are found, so find walks stay short.
     volatile int* hint = v.sroot;
     unsigned rechecks = 0;
     int err = 0;
-    const int nblk = (n + 31) >> 5;
-    const int per = (nblk + nw - 1) / nw;  // contiguous blocks per warp: L1 reuse
-    const int b0 = min(gw * per, nblk), b1 = min(b0 + per, nblk);
-    for (int blk = b0; blk < b1; ++blk) {
-        const int ph = blk * 32 + lane;
-        const bool valid = ph < n;
+    for (int itx = it0; itx < it1; ++itx) {
+        const int2 item = v.items[itx];
+        const int start = item.x, len = item.y;
+        const bool hv = lane < len;
         float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
-        unsigned long long key = ~0ull;
         bool hcore = false;
-        int hr = 0;
-        if (valid) {
-            h = spt[ph];
-            key = skey[ph];
-            hcore = scnt[ph] >= v.min_pts;
-            if (hcore) hr = hint[ph];
+        if (hv) {
+            h = spt[start + lane];
+            hcore = scnt[start + lane] >= v.min_pts;
         }
-        if (!__any_sync(kFull, hcore)) continue;
-        // Cells of this block: a lane whose key differs from its left
-        // neighbour's starts a cell; k = the lane's cell index.
-        const unsigned long long kp = __shfl_up_sync(kFull, key, 1);
-        const bool first = valid && (lane == 0 || kp != key);
-        const unsigned cmask = __ballot_sync(kFull, first);
-        const int m = __popc(cmask);
-        const int k = __popc(cmask & ((2u << lane) - 1u)) - 1;
+        const unsigned hmask = __ballot_sync(kFull, hcore);
+        if (!hmask) continue;
         __syncwarp();
-        if (first) cell_key[wib][k] = key;
-        __syncwarp();
-        // Row ranges of every (cell, row): the row's three cells (last axis
-        // -1, 0, +1) have consecutive keys, so they form one contiguous range.
-        for (int t = lane; t < m * kRows; t += 32) {
-            const int kc = t / kRows, row = t - kc * kRows;
-            const unsigned long long ck = cell_key[wib][kc];
-            const long long c2 = (long long)(ck & ((1ull << v.shift[1]) - 1ull));
-            const long long c1 = (long long)((ck >> v.shift[1]) & ((1ull << (v.shift[0] - v.shift[1])) - 1ull));
-            const long long c0 = (long long)(ck >> v.shift[0]);
-            long long q0 = c0, q1 = c1;
-            if (DIM == 1) {
-                // single row along axis 0
-            } else if (DIM == 2) {
-                q0 += row - 1;
-            } else {
-                q0 += row / 3 - 1;
-                q1 += row % 3 - 1;
+        if (hcore) rh[lane] = hint[start + lane];
+        home_pt[wib][lane] = h;
+        const int hmin = start + __ffs(hmask) - 1;
+        int rs, re;
+        row_ranges<DIM>(v, T, gen, skey[start], lane, rs, re);
+        const int total = candidate_stream<DIM>(rs, re, hmin + 1, lane, rstart[wib], rpre[wib]);
+        int r = 0;
+        for (int base = 0; base < total; base += 32) {
+            const int idx = base + lane;
+            int pos = 0, qh = 0;
+            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+            bool qc = false;
+            if (idx < total) {
+                pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
+                qc = scnt[pos] >= v.min_pts;
+                if (qc) {
+                    q = spt[pos];
+                    qh = hint[pos];
+                }
             }
-            int rs = INT_MAX, re = INT_MIN;
-            const bool row_ok = q0 >= 0 && q0 < v.ext[0] && q1 >= 0 && q1 < v.ext[1];
-#pragma unroll
-            for (int dz = -1; dz <= 1; ++dz) {
-                long long a0 = q0, a1 = q1, a2 = c2;
-                if (DIM == 1) a0 += dz;
-                else if (DIM == 2) a1 = c1 + dz;
-                else a2 += dz;
-                const bool ok = row_ok && a0 >= 0 && a0 < v.ext[0] && a1 >= 0 && a1 < v.ext[1] && a2 >= 0 &&
-                                a2 < v.ext[2];
-                if (ok) {
-                    const unsigned long long nk = ((unsigned long long)a0 << v.shift[0]) |
-                                                  ((unsigned long long)a1 << v.shift[1]) | (unsigned long long)a2;
-                    const int2 g = table_find(T, v.pmask, v.pbits, tag_of(nk, gen));
-                    if (g.y > g.x) {
-                        rs = min(rs, g.x);
-                        re = max(re, g.y);
+            if (!__any_sync(kFull, qc)) continue;
+            // Pairs whose hints already agree are in one set: no test, no link.
+            unsigned adj = 0;
+            unsigned mm = hmask;
+            while (mm) {
+                const int hi = __ffs(mm) - 1;
+                mm &= mm - 1;
+                if (qc && pos > start + hi && qh != rh[hi] && is_nbr<MODE, DIM>(v, hpt[hi], q, rechecks))
+                    adj |= 1u << hi;
+            }
+            if (adj) {
+                int rq = uf_find(parent, qh);
+                while (adj) {
+                    const int hi = __ffs(adj) - 1;
+                    adj &= adj - 1;
+                    const int ra = rh[hi];
+                    if (ra != rq) {
+                        rq = uf_link(parent, ra, rq, err);
+                        rh[hi] = rq;  // an ancestor of both points (benign race)
                     }
                 }
+                if (rq != qh) hint[pos] = rq;
             }
-            if (re == INT_MIN) rs = re = 0;
-            cell_rows[wib][kc][row] = make_int2(rs, re);
+            __syncwarp();
         }
-        __syncwarp();
-        // Each core home walks its rows above its own position.
-        const int2* rows = cell_rows[wib][valid ? k : 0];
-        int r = 0, a = 0, e = 0;
-        if (hcore) {
-            for (; r < kRows; ++r) {
-                a = max(rows[r].x, ph + 1);
-                e = rows[r].y;
-                if (a < e) break;
-            }
-        } else {
-            r = kRows;
-        }
-        const int hr_in = hr;
-        while (__any_sync(kFull, r < kRows)) {
-            if (r < kRows) {
-                const float4 q = spt[a];
-                const int qh = hint[a];
-                if (qh != hr && scnt[a] >= v.min_pts && is_nbr<MODE, DIM>(v, h, q, rechecks)) {
-                    const int rq = uf_find(parent, qh);
-                    hr = uf_link(parent, hr, rq, err);
-                    if (hr != qh) hint[a] = hr;
-                }
-                if (++a >= e) {
-                    for (++r; r < kRows; ++r) {
-                        a = rows[r].x;
-                        e = rows[r].y;
-                        if (a < e) break;
-                    }
-                }
-            }
-        }
-        if (hcore && hr != hr_in) hint[ph] = hr;
-        __syncwarp();
+        if (hcore) hint[start + lane] = rh[lane];
     }
     flush_stats(v, rechecks, err, lane);
 }
@@ -1047,8 +1009,8 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
             const int per_block = kClusterThreads / 32;
             const int need = (v.max_items + per_block - 1) / per_block;  // one warp per item at most
             const int blocks = max(1, min(sms * 6, need));
-            if (phase == kPhaseUnion)  // one resident wave at 4 blocks per SM
-                RTDBS_DISPATCH(precision, v.dim, k_union, max(1, min(sms * 4, need)), kClusterThreads, s, v);
+            if (phase == kPhaseUnion)
+                RTDBS_DISPATCH(precision, v.dim, k_union, blocks, kClusterThreads, s, v);
             else
                 RTDBS_DISPATCH(precision, v.dim, k_label, blocks, kClusterThreads, s, v, advance);
             break;
