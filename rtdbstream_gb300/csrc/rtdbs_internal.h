@@ -37,6 +37,7 @@ constexpr int kSortRun = 1024;     // words per radix-sort CTA (one per thread)
 constexpr int kMaxRuns = kChunkMax / kSortRun;
 constexpr int kBuildThreads = 512;
 constexpr int kClusterThreads = 256;
+constexpr int kBatch = 8;          // work items a clustering warp takes at a time
 constexpr int kMaxIter = 1 << 20;  // bound on every device-side retry loop
 
 // Bits of Ctl::err.
@@ -56,8 +57,10 @@ struct Ctl {
     int ncells;                // cells of the current grid
     int err;                   // kErr* bits
     int pad0;
+    int union_next;            // next work item handed out by k_union
+    int label_next;            // next work item handed out by k_label
     unsigned long long band_rechecks;
-    long long reserved[4];
+    long long reserved[3];
 };
 
 // Everything a kernel needs for one stream, passed by value.

@@ -486,6 +486,8 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
         v.ctl->nocc[dst] = n_new;
         v.ctl->nitems = 0;
         v.ctl->ncells = 0;
+        v.ctl->union_next = 0;
+        v.ctl->label_next = 0;
     }
     // Table generations wrap every kGenMod builds of a table: clear it then.
     if (b >= 2 && ((b >> 1) % (long long)kGenMod) == 0) {
@@ -778,14 +780,10 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     volatile int* rh = home_root[wib];
     const float4* hpt = home_pt[wib];
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
     const long long b = v.ctl->b;
     const int cur = (int)(b & 1);
     const unsigned gen = gen_of_build(b);
     const int nitems = min(v.ctl->nitems, v.max_items);
-    const int per = (nitems + nw - 1) / nw;
-    const int it0 = min(gw * per, nitems), it1 = min(it0 + per, nitems);
     const float4* spt = v.spt[cur];
     const int* scnt = v.scnt[cur];
     const unsigned long long* skey = v.skey[cur];
@@ -797,8 +795,19 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
     volatile int* hint = v.sroot;
     unsigned rechecks = 0;
     int err = 0;
-    for (int itx = it0; itx < it1; ++itx) {
-        const int2 item = v.items[itx];
+    // Warps take batches of kBatch consecutive work items (neighbouring
+    // cells: candidate loads reuse L1) from a counter, so uneven items do not
+    // leave warps idle at the end.
+    int it1 = 0;
+    for (int itx = nitems;;) {
+        if (itx >= it1) {
+            int got = 0;
+            if (lane == 0) got = atomicAdd(&v.ctl->union_next, kBatch);
+            itx = __shfl_sync(kFull, got, 0);
+            if (itx >= nitems) break;
+            it1 = min(itx + kBatch, nitems);
+        }
+        const int2 item = v.items[itx++];
         const int start = item.x, len = item.y;
         const bool hv = lane < len;
         float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -863,6 +872,7 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
 // Root of every core point by sorted position (-1 for non-core points),
 // walked from the position's root hint.
 __global__ void k_flatten(View v) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) v.ctl->label_next = 0;  // k_label's queue; not read here
     const int cur = (int)(v.ctl->b & 1);
     const int n = v.ctl->nocc[cur];
     const int* scnt = v.scnt[cur];
@@ -878,21 +888,25 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advanc
     __shared__ float4 home_pt[kClusterThreads / 32][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const float4* hpt = home_pt[wib];
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
     const long long b = v.ctl->b;
     const int cur = (int)(b & 1);
     const unsigned gen = gen_of_build(b);
     const int nitems = min(v.ctl->nitems, v.max_items);
-    const int per = (nitems + nw - 1) / nw;
-    const int it0 = min(gw * per, nitems), it1 = min(it0 + per, nitems);
     const float4* spt = v.spt[cur];
     const int* sroot = v.sroot;
     const unsigned long long* skey = v.skey[cur];
     const ulonglong2* T = v.table[cur];
     unsigned rechecks = 0;
-    for (int itx = it0; itx < it1; ++itx) {
-        const int2 item = v.items[itx];
+    int it1 = 0;
+    for (int itx = nitems;;) {
+        if (itx >= it1) {
+            int got = 0;
+            if (lane == 0) got = atomicAdd(&v.ctl->label_next, kBatch);
+            itx = __shfl_sync(kFull, got, 0);
+            if (itx >= nitems) break;
+            it1 = min(itx + kBatch, nitems);
+        }
+        const int2 item = v.items[itx++];
         const int start = item.x, len = item.y;
         const bool hv = lane < len;
         float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -944,7 +958,10 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advanc
         }
     }
     flush_stats(v, rechecks, 0, lane);
-    if (advance && blockIdx.x == 0 && threadIdx.x == 0) v.ctl->slide += 1;  // no reader here
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        v.ctl->union_next = 0;                // the next clustering's queue; not read here
+        if (advance) v.ctl->slide += 1;       // no reader here
+    }
 }
 
 __global__ void k_counts_by_slot(View v, int* nn) {

@@ -183,6 +183,20 @@ def test_slide_async_device_buffers():
     eng.close()
 
 
+def test_cluster_twice_without_slide():
+    pts = wl.gaussian_mixture(4_000 + 1_000, dim=3, k=6, box=15.0, seed=15)
+    with Engine(3, 4_000, 1_000, 1.0, 5) as eng:
+        eng.load_window(pts[:4_000])
+        a = eng.cluster()
+        b = eng.cluster()
+        c = eng.slide(pts[4_000:])
+        d = eng.cluster()
+    exp0 = O.window_grid(pts[:4_000], 1.0, 5, O.MODE_FP64)
+    exp1 = O.window_grid(O.window_of(pts, 4_000, 1_000, 1), 1.0, 5, O.MODE_FP64)
+    for (lab, cid), (_, elab, ecid, _) in ((a, exp0), (b, exp0), (c, exp1), (d, exp1)):
+        assert np.array_equal(lab, elab) and np.array_equal(cid, ecid)
+
+
 def test_api_errors():
     with pytest.raises(RtdbsError) as ei:
         Engine(2, 100, 30, 0.5, 4)
