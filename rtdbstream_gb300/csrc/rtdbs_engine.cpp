@@ -527,7 +527,7 @@ int rtdbs_get_stats(rtdbs_engine* e, rtdbs_stats* s) {
     s->device_bytes = (int64_t)e->dev_bytes;
     const int nchunks = (e->p.stride + e->chunk - 1) / e->chunk;
     s->chunks_per_slide = nchunks;
-    s->launches_per_slide = nchunks * rtdbs::kChunkPhases + 3;
+    s->launches_per_slide = nchunks * (rtdbs::kChunkPhases + 1) + 3;  // sort phase = 2 kernels
     return RTDBS_OK;
 }
 

@@ -32,9 +32,7 @@ constexpr unsigned long long kKeyMask = (1ull << kKeyBitsMax) - 1ull;
 constexpr unsigned kGenMod = 16383;  // table generations 1..16383 (tag = gen << 50 | key)
 constexpr int kMergeTile = 1024;   // old entries per merge block
 constexpr int kMergeThreads = 256;
-constexpr int kMergeNewCap = 1024;  // new words of one merge tile staged in shared memory
 constexpr int kSortRun = 1024;     // words per radix-sort CTA (one per thread)
-constexpr int kMaxRuns = kChunkMax / kSortRun;
 constexpr int kBuildThreads = 512;
 constexpr int kClusterThreads = 256;
 constexpr int kBatch = 8;          // work items a clustering warp takes at a time

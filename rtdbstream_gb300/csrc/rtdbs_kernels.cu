@@ -7,8 +7,9 @@
 //     k_ingest  new points -> ring slots + cell keys; expired points saved
 //               (reference: H2D 2289 + compute_cell_id, src/dbscan/aabb.cu:589-610)
 //     k_sort    LSD radix sort of the new and of the expired (cell key, slot)
-//               words in runs of 1024, one CTA per run (reference:
-//               sortByCellIdAndOrder, src/dbscan/thrust_helper.cu:21-29)
+//               words in runs of 1024, one CTA per run, then k_runmerge
+//               ranks the runs into one list (reference: sortByCellIdAndOrder,
+//               src/dbscan/thrust_helper.cu:21-29)
 //     k_decr    exact -1 on the neighbour counts of every survivor within Eps
 //               of an expired point, on the old grid
 //     k_merge   old sorted window minus expired plus new, one pass, merge-path
@@ -374,11 +375,10 @@ __global__ void __launch_bounds__(kSortRun) k_sort(View v, int c, int init) {
     const int r0 = blockIdx.x * kSortRun;
     const int len = min(kSortRun, c - r0);
     if (len <= 0) return;
-    const unsigned long long* in = (which ? v.xsort : v.nsort) + r0;
-    unsigned long long* out = (which ? v.xword : v.nword) + r0;
+    unsigned long long* run = (which ? v.xsort : v.nsort) + r0;  // sorted in place
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const unsigned lt = lanemask_lt(lane);
-    unsigned long long it = tid < len ? in[tid] : ~0ull;
+    unsigned long long it = tid < len ? run[tid] : ~0ull;
     for (int pass = 0; pass < v.sort_passes; ++pass) {
         const int shift = kOffBits + 8 * pass;
 #pragma unroll
@@ -412,7 +412,37 @@ __global__ void __launch_bounds__(kSortRun) k_sort(View v, int c, int init) {
         __syncthreads();
         it = buf[tid];
     }
-    if (tid < len) out[tid] = it;
+    if (tid < len) run[tid] = it;
+}
+
+// Merges the sorted runs of kSortRun words into one sorted list: a word's
+// rank is its index in its run plus the words below it in every other run
+// (words are distinct, so ranks are too).  y = 0: new words, 1: expired.
+__global__ void k_runmerge(View v, int c, int init) {
+    const int which = blockIdx.y;
+    if (which == 1 && init) return;
+    const unsigned long long* runs = which ? v.xsort : v.nsort;
+    unsigned long long* out = which ? v.xword : v.nword;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c) return;
+    const unsigned long long w = runs[i];
+    const int nruns = (c + kSortRun - 1) / kSortRun;
+    const int own = i / kSortRun;
+    int rank = i - own * kSortRun;
+    for (int r = 0; r < nruns; ++r) {
+        if (r == own) continue;
+        const unsigned long long* run = runs + r * kSortRun;
+        int lo = 0, hi = min(kSortRun, c - r * kSortRun);
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (run[mid] < w)
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        rank += lo;
+    }
+    out[rank] = w;
 }
 
 // -1 on the count of every surviving neighbour of each expired point (old grid).
@@ -466,16 +496,13 @@ __device__ __forceinline__ int count_words_less(const unsigned long long* words,
 }
 
 // Old sorted window minus the expired slots [el, el+c), merged with the c
-// new entries (held as sorted runs of kSortRun words); tile t of the old
-// window goes to output offset ts - (#expired before ts) + (#new before
-// old[ts]), each count summed over the runs.
+// new entries; tile t of the old window goes to output offset
+// ts - (#expired before ts) + (#new before old[ts]).
 __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, int init) {
     __shared__ unsigned long long tkey[kMergeTile];
     __shared__ int tslot[kMergeTile];
     __shared__ int spre[kMergeTile + 1];
     __shared__ unsigned wsum[32];
-    __shared__ int rn0[kMaxRuns], rn1[kMaxRuns], rx[kMaxRuns];
-    __shared__ unsigned long long tnew[kMergeNewCap];
     const long long b = v.ctl->b;
     const int src = (int)((b - 1) & 1), dst = (int)(b & 1);
     const int n_old = v.ctl->nocc[src];
@@ -507,38 +534,23 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
     unsigned long long* dkey = v.skey[dst];
     float4* dpt = v.spt[dst];
     int* dcnt = v.scnt[dst];
-    const int nruns = (c + kSortRun - 1) / kSortRun;
 
-    // Per run: the range of new words that fall in this tile, and the expired
-    // words before it.
-    if (tid < nruns) {
-        const int rb = tid * kSortRun, rl = min(kSortRun, c - rb);
-        int a = 0, z = rl, x = 0;
-        if (tlen > 0) {
-            const unsigned long long k0 = okey[ts];
-            const int s0 = slot_of(opt[ts]);
-            if (t > 0) a = count_words_less(v.nword + rb, rl, el, k0, s0);
-            if (!init) x = count_words_less(v.xword + rb, rl, el, k0, s0);
-            if (t < ntiles - 1) z = count_words_less(v.nword + rb, rl, el, okey[te], slot_of(opt[te]));
-        }
-        rn0[tid] = rb + a;
-        rn1[tid] = rb + z;
-        rx[tid] = x;
+    int jt0 = 0, jt1 = c, e0 = 0;
+    if (tlen > 0) {
+        const unsigned long long k0 = okey[ts];
+        const int s0 = slot_of(opt[ts]);
+        if (t > 0) jt0 = count_words_less(v.nword, c, el, k0, s0);
+        if (!init) e0 = count_words_less(v.xword, c, el, k0, s0);
+        if (t < ntiles - 1) jt1 = count_words_less(v.nword, c, el, okey[te], slot_of(opt[te]));
     }
-    // tile -> shared memory
+    const int base = ts - e0 + jt0;
+
+    // tile -> shared memory; survivor prefix in item order
     for (int i = tid; i < tlen; i += kMergeThreads) {
         tkey[i] = okey[ts + i];
         tslot[i] = slot_of(opt[ts + i]);
     }
     __syncthreads();
-    int jt0 = 0, e0 = 0;
-    for (int r = 0; r < nruns; ++r) {
-        jt0 += rn0[r] - r * kSortRun;
-        e0 += rx[r];
-    }
-    const int base = ts - e0 + jt0;
-
-    // survivor prefix in item order
     unsigned flags[4];
     unsigned cnt = 0;
 #pragma unroll
@@ -579,37 +591,12 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
     }
     __syncthreads();
 
-    // The tile's new words from all runs, merged in shared memory when they fit.
-    int m = 0;
-    for (int r = 0; r < nruns; ++r) m += rn1[r] - rn0[r];
-    const bool staged = m <= kMergeNewCap;
-    if (staged) {
-        for (int r = 0; r < nruns; ++r) {
-            for (int q = rn0[r] + tid; q < rn1[r]; q += kMergeThreads) {
-                const unsigned long long wd = v.nword[q];
-                const unsigned long long key = wd >> kOffBits;
-                const int slot = el + (int)(wd & ((1u << kOffBits) - 1));
-                int rank = q - rn0[r];
-                for (int r2 = 0; r2 < nruns; ++r2)
-                    if (r2 != r && rn1[r2] > rn0[r2])
-                        rank += count_words_less(v.nword + rn0[r2], rn1[r2] - rn0[r2], el, key, slot);
-                tnew[rank] = wd;
-            }
-        }
-        __syncthreads();
-    }
-
     // survivors (coalesced, item order i = tid + 256 k)
+    const int m = jt1 - jt0;
     for (int i = tid; i < tlen; i += kMergeThreads) {
         const int s = tslot[i];
         if (!(init || s < el || s >= el + c)) continue;
-        int lessnew = 0;
-        if (staged) {
-            if (m > 0) lessnew = count_words_less(tnew, m, el, tkey[i], s);
-        } else {
-            for (int r = 0; r < nruns; ++r)
-                if (rn1[r] > rn0[r]) lessnew += count_words_less(v.nword + rn0[r], rn1[r] - rn0[r], el, tkey[i], s);
-        }
+        const int lessnew = m > 0 ? count_words_less(v.nword + jt0, m, el, tkey[i], s) : 0;
         const int o = base + spre[i] + lessnew;
         if (o < 0 || o >= n_new) {
             atomicOr(&v.ctl->err, kErrChunk);
@@ -621,40 +608,29 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
         v.sroot[o] = s;
         v.parent[s] = s;
     }
-    // new entries of this tile (merged order from shared memory, or run by run)
-    const int nq = staged ? m : 0;
-    for (int r = staged ? nruns : 0; r <= nruns; ++r) {
-        const bool from_smem = r == nruns;
-        if (from_smem && !staged) break;
-        const int q0 = from_smem ? 0 : rn0[r], q1 = from_smem ? nq : rn1[r];
-        for (int q = q0 + tid; q < q1; q += kMergeThreads) {
-            const unsigned long long wd = from_smem ? tnew[q] : v.nword[q];
-            const unsigned long long key = wd >> kOffBits;
-            const int slot = el + (int)(wd & ((1u << kOffBits) - 1));
-            int rank = q - q0;  // new entries of this tile below it, all runs
-            if (!from_smem)
-                for (int r2 = 0; r2 < nruns; ++r2)
-                    if (r2 != r && rn1[r2] > rn0[r2])
-                        rank += count_words_less(v.nword + rn0[r2], rn1[r2] - rn0[r2], el, key, slot);
-            int lo = 0, hi = tlen;  // old tile entries below (key, slot)
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (tuple_less(tkey[mid], tslot[mid], key, slot))
-                    lo = mid + 1;
-                else
-                    hi = mid;
-            }
-            const int o = base + rank + spre[lo];
-            if (o < 0 || o >= n_new || slot < 0 || slot >= v.W) {
-                atomicOr(&v.ctl->err, kErrChunk);
-                continue;
-            }
-            dkey[o] = key;
-            dpt[o] = v.ring[slot];
-            dcnt[o] = 0;
-            v.sroot[o] = slot;
-            v.parent[slot] = slot;
+    // new entries of this tile
+    for (int q = jt0 + tid; q < jt1; q += kMergeThreads) {
+        const unsigned long long wd = v.nword[q];
+        const unsigned long long key = wd >> kOffBits;
+        const int slot = el + (int)(wd & ((1u << kOffBits) - 1));
+        int lo = 0, hi = tlen;  // old tile entries below (key, slot)
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (tuple_less(tkey[mid], tslot[mid], key, slot))
+                lo = mid + 1;
+            else
+                hi = mid;
         }
+        const int o = base + (q - jt0) + spre[lo];
+        if (o < 0 || o >= n_new || slot < 0 || slot >= v.W) {
+            atomicOr(&v.ctl->err, kErrChunk);
+            continue;
+        }
+        dkey[o] = key;
+        dpt[o] = v.ring[slot];
+        dcnt[o] = 0;
+        v.sroot[o] = slot;
+        v.parent[slot] = slot;
     }
 }
 
@@ -1007,6 +983,7 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
             break;
         case kPhaseSort:
             k_sort<<<dim3((c + kSortRun - 1) / kSortRun, init ? 1 : 2), kSortRun, 0, s>>>(v, c, init);
+            k_runmerge<<<dim3((c + 255) / 256, init ? 1 : 2), 256, 0, s>>>(v, c, init);
             break;
         case kPhaseDecrement:
             if (!init) RTDBS_DISPATCH(precision, v.dim, k_decr, warp_blocks, 256, s, v, j, c);
