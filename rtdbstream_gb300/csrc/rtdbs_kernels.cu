@@ -37,6 +37,7 @@
 // reference's CPU checker (src/dbscan/util.cpp:308-316).
 #include "rtdbs_internal.h"
 
+#include <atomic>
 #include <climits>
 #include <cstdint>
 
@@ -417,21 +418,26 @@ __global__ void __launch_bounds__(kSortRun) k_sort(View v, int c, int init) {
 
 // Merges the sorted runs of kSortRun words into one sorted list: a word's
 // rank is its index in its run plus the words below it in every other run
-// (words are distinct, so ranks are too).  y = 0: new words, 1: expired.
-__global__ void k_runmerge(View v, int c, int init) {
+// (words are distinct, so ranks are too).  Block (r, y) ranks run r of the
+// new (y = 0) or expired (y = 1) words; all c words are staged in shared
+// memory first, so the binary searches stay on chip.
+__global__ void __launch_bounds__(kSortRun) k_runmerge(View v, int c, int init) {
+    extern __shared__ unsigned long long words[];
     const int which = blockIdx.y;
     if (which == 1 && init) return;
     const unsigned long long* runs = which ? v.xsort : v.nsort;
     unsigned long long* out = which ? v.xword : v.nword;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int i = threadIdx.x; i < c; i += blockDim.x) words[i] = runs[i];
+    __syncthreads();
+    const int own = blockIdx.x;
+    const int i = own * kSortRun + threadIdx.x;
     if (i >= c) return;
-    const unsigned long long w = runs[i];
+    const unsigned long long w = words[i];
     const int nruns = (c + kSortRun - 1) / kSortRun;
-    const int own = i / kSortRun;
-    int rank = i - own * kSortRun;
+    int rank = threadIdx.x;
     for (int r = 0; r < nruns; ++r) {
         if (r == own) continue;
-        const unsigned long long* run = runs + r * kSortRun;
+        const unsigned long long* run = words + r * kSortRun;
         int lo = 0, hi = min(kSortRun, c - r * kSortRun);
         while (lo < hi) {
             const int mid = (lo + hi) >> 1;
@@ -948,6 +954,19 @@ __global__ void k_counts_by_slot(View v, int* nn) {
 }
 
 int g_num_sms = 0;
+std::atomic<unsigned long long> g_runmerge_ready{0};  // one bit per device
+
+// k_runmerge stages up to kChunkMax words (128 KB) in dynamic shared memory;
+// allow that once per device (a host-side attribute, not a stream operation).
+void ensure_runmerge_smem() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+    const unsigned long long bit = 1ull << dev;
+    if (g_runmerge_ready.load() & bit) return;
+    if (cudaFuncSetAttribute(k_runmerge, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(unsigned long long) * kChunkMax)) == cudaSuccess)
+        g_runmerge_ready.fetch_or(bit);
+}
 
 }  // namespace
 
@@ -983,7 +1002,9 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
             break;
         case kPhaseSort:
             k_sort<<<dim3((c + kSortRun - 1) / kSortRun, init ? 1 : 2), kSortRun, 0, s>>>(v, c, init);
-            k_runmerge<<<dim3((c + 255) / 256, init ? 1 : 2), 256, 0, s>>>(v, c, init);
+            ensure_runmerge_smem();
+            k_runmerge<<<dim3((c + kSortRun - 1) / kSortRun, init ? 1 : 2), kSortRun,
+                         sizeof(unsigned long long) * c, s>>>(v, c, init);
             break;
         case kPhaseDecrement:
             if (!init) RTDBS_DISPATCH(precision, v.dim, k_decr, warp_blocks, 256, s, v, j, c);
