@@ -54,6 +54,7 @@ extern "C" {
 #define RTDBS_ERR_DEVICE    -5  /* a device-side bound was hit (hash probe, union-find retry,
                                    work-list capacity); the engine must be reloaded */
 #define RTDBS_ERR_NO_DEVICE -6  /* no CUDA device / library built without one */
+#define RTDBS_ERR_BUDGET    -7  /* pool admission refused: HBM budget or stream slots exhausted */
 
 /* Precision modes. */
 #define RTDBS_PREC_FP64 0
@@ -205,6 +206,65 @@ RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int32_t n, int
  * events; synchronous.  Results are identical to an ordinary slide. */
 RTDBS_API int rtdbs_slide_profiled(rtdbs_engine* engine, const float* d_new_points,
                                    rtdbs_phase_times* times);
+
+/* ------------------------------------------------------------------ pools
+ * A pool slides many independent streams together: one launch per kernel
+ * phase covers every stream of a round (each with its own W, S, dim, Eps,
+ * MinPts and precision), and a round whose stream set repeats is one CUDA
+ * graph replay.  The reference runs one stream per process; this is the
+ * batched / serving extension of its slide loop.  Streams are admitted
+ * against an HBM budget and can be added and removed between rounds. */
+
+typedef struct rtdbs_pool rtdbs_pool;
+
+typedef struct rtdbs_pool_params {
+    int32_t device;            /* CUDA device ordinal */
+    int32_t flags;             /* RTDBS_FLAG_NO_GRAPH: launch rounds directly */
+    int32_t max_streams;       /* stream slots (default 1024) */
+    int32_t reserved0;
+    int64_t hbm_budget_bytes;  /* admission limit on the streams' device memory; 0 = none */
+    int64_t reserved[6];
+} rtdbs_pool_params;
+
+typedef struct rtdbs_pool_stats {
+    int64_t streams;           /* admitted streams */
+    int64_t bytes_in_use;      /* device memory of the admitted streams */
+    int64_t budget_bytes;
+    int64_t rounds;            /* rounds launched */
+    int64_t graph_replays;     /* rounds that replayed a cached graph */
+    int32_t launches_per_round;
+    int32_t reserved0;
+    int64_t reserved[4];
+} rtdbs_pool_stats;
+
+/* Device bytes a stream with these parameters occupies (its admission cost). */
+RTDBS_API int rtdbs_stream_bytes(const rtdbs_params* params, int64_t* bytes);
+RTDBS_API int rtdbs_pool_params_init(rtdbs_pool_params* params);
+RTDBS_API int rtdbs_pool_create(const rtdbs_pool_params* params, void* cuda_stream, rtdbs_pool** out);
+RTDBS_API int rtdbs_pool_destroy(rtdbs_pool* pool);
+/* Admits one stream (RTDBS_ERR_BUDGET when it does not fit); *stream_id is its slot. */
+RTDBS_API int rtdbs_pool_add_stream(rtdbs_pool* pool, const rtdbs_params* params, int32_t* stream_id);
+/* Frees the stream's slot and memory (waits for the pool's stream first). */
+RTDBS_API int rtdbs_pool_remove_stream(rtdbs_pool* pool, int32_t stream_id);
+RTDBS_API int rtdbs_pool_load_window(rtdbs_pool* pool, int32_t stream_id, const float* points,
+                                     int points_on_device);
+/* One round: each of the n listed (distinct, loaded) streams slides by its
+ * stride.  d_points (device) holds their new points back to back in the
+ * listed order, S_i * dim_i floats each.  Stream-ordered; results are then in
+ * each stream's device buffers (rtdbs_pool_outputs). */
+RTDBS_API int rtdbs_pool_slide(rtdbs_pool* pool, int32_t n, const int32_t* stream_ids,
+                               const float* d_points);
+/* Waits for the pool's stream; RTDBS_ERR_DEVICE if any stream hit a device bound. */
+RTDBS_API int rtdbs_pool_sync(rtdbs_pool* pool);
+RTDBS_API int rtdbs_pool_outputs(rtdbs_pool* pool, int32_t stream_id, int32_t** d_label,
+                                 int32_t** d_cluster_id);
+/* Copies one stream's latest label[W] and cluster_id[W] (host or device
+ * memory per on_device); waits for the pool's stream. */
+RTDBS_API int rtdbs_pool_read_outputs(rtdbs_pool* pool, int32_t stream_id, int32_t* label,
+                                      int32_t* cluster_id, int on_device);
+/* The stream's engine, for the per-engine queries (counts, stats, cluster). */
+RTDBS_API int rtdbs_pool_engine(rtdbs_pool* pool, int32_t stream_id, rtdbs_engine** engine);
+RTDBS_API int rtdbs_pool_get_stats(rtdbs_pool* pool, rtdbs_pool_stats* stats);
 
 #ifdef __cplusplus
 }

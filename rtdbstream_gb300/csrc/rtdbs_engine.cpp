@@ -163,7 +163,14 @@ void set_band(View& v, double eps) {
     v.r2f = r * r;
 }
 
-int allocate(rtdbs_engine* e) {
+struct Part {
+    void** ptr;
+    size_t bytes;
+};
+
+// Buffer layout of one engine (sizes from W, S, dim); returns the bytes of
+// the single device block that holds it.
+size_t plan_layout(rtdbs_engine* e, std::vector<Part>& parts) {
     const int W = e->p.window, S = e->p.stride, dim = e->p.dim;
     View& v = e->v;
     e->chunk = std::min(S, rtdbs::kChunkMax);
@@ -179,12 +186,7 @@ int allocate(rtdbs_engine* e) {
     v.pbits = pbits;
     v.pmask = (unsigned)(P - 1);
     v.max_items = W + W / 32 + 64;
-
-    struct Part {
-        void** ptr;
-        size_t bytes;
-    };
-    std::vector<Part> parts = {
+    parts = {
         {(void**)&v.ring, sizeof(float4) * W},
         {(void**)&v.kslot, sizeof(unsigned long long) * W},
         {(void**)&v.skey[0], sizeof(unsigned long long) * W},
@@ -210,6 +212,14 @@ int allocate(rtdbs_engine* e) {
     };
     size_t total = 0;
     for (auto& q : parts) total += align_up(q.bytes, 256);
+    return total;
+}
+
+int allocate(rtdbs_engine* e) {
+    std::vector<Part> parts;
+    const size_t total = plan_layout(e, parts);
+    View& v = e->v;
+    const unsigned long long P = (unsigned long long)v.pmask + 1;
     CUDA_TRY(cudaMalloc(&e->dev_block, total));
     e->dev_bytes = total;
     char* base = static_cast<char*>(e->dev_block);
@@ -360,6 +370,7 @@ int rtdbs_create(const rtdbs_params* params, void* cuda_stream, rtdbs_engine** o
     v.S = p.stride;
     v.min_pts = p.min_pts;
     v.units = p.window / p.stride;
+    v.precision = p.precision;
     set_band(v, p.eps);
     int rc = allocate(e);
     if (rc == RTDBS_OK) {
@@ -595,6 +606,385 @@ int rtdbs_slide_profiled(rtdbs_engine* e, const float* d_new_points, rtdbs_phase
     for (auto& x : ev)
         if (x) cudaEventDestroy(x);
     return rc;
+}
+
+
+// ====================================================================== pool
+
+int rtdbs_stream_bytes(const rtdbs_params* params, int64_t* bytes) {
+    if (!params || !bytes) return fail(RTDBS_ERR_INVALID, "params/bytes is NULL");
+    if (params->window <= 0 || params->stride <= 0 || params->dim < 1 || params->dim > 3)
+        return fail(RTDBS_ERR_INVALID, "bad window/stride/dim");
+    rtdbs_engine tmp;
+    tmp.p = *params;
+    std::vector<Part> parts;
+    *bytes = (int64_t)plan_layout(&tmp, parts);
+    return RTDBS_OK;
+}
+
+}  // extern "C"
+
+struct rtdbs_pool {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int flags = 0;
+    int64_t budget = 0;  // 0: unlimited
+    int64_t used = 0;
+    int capacity = 0;
+    std::vector<rtdbs_engine*> eng;   // slot -> engine (nullptr: free)
+    std::vector<char> loaded;
+    View* d_views = nullptr;          // one View per slot
+    Ctl* d_ctls = nullptr;            // every stream's control block, contiguous
+    Ctl* h_ctls = nullptr;            // pinned mirror
+    char* d_tables = nullptr;         // items + prefixes of the cached round shape
+    size_t tables_cap = 0;
+    float* d_input = nullptr;         // the round's new points, back to back
+    size_t input_cap = 0;             // floats
+    std::vector<int> shape_ids;       // stream set the tables / graph were built for
+    cudaGraphExec_t graph = nullptr;
+    // launch plan of the cached shape
+    struct Launch {
+        int phase;
+        size_t items_off, prefix_off;  // byte offsets into d_tables
+        int n, blocks, max_c;
+    };
+    std::vector<Launch> plan;
+    std::vector<size_t> input_off;    // per listed stream, float offset into d_input
+    size_t input_floats = 0;
+    int64_t rounds = 0, graph_replays = 0;
+};
+
+namespace {
+
+void pool_drop_shape(rtdbs_pool* p) {
+    if (p->graph) {
+        cudaGraphExecDestroy(p->graph);
+        p->graph = nullptr;
+    }
+    p->shape_ids.clear();
+    p->plan.clear();
+}
+
+// Builds (and uploads) the launch tables of one round over `ids`.
+int pool_build_shape(rtdbs_pool* p, const std::vector<int>& ids) {
+    using rtdbs::BatchItem;
+    const int n = (int)ids.size();
+    std::vector<size_t> off(n);
+    size_t floats = 0;
+    int maxchunks = 0;
+    for (int i = 0; i < n; ++i) {
+        const rtdbs_engine* e = p->eng[ids[i]];
+        off[i] = floats;
+        floats += (size_t)e->p.stride * e->p.dim;
+        maxchunks = std::max(maxchunks, (e->p.stride + e->chunk - 1) / e->chunk);
+    }
+    if (floats > p->input_cap) {
+        if (p->d_input) cudaFree(p->d_input);
+        p->d_input = nullptr;
+        CUDA_TRY(cudaMalloc((void**)&p->d_input, sizeof(float) * floats));
+        p->input_cap = floats;
+    }
+    // host image of the tables: per chunk step j an item array, then every
+    // launch's prefix array
+    std::vector<char> img;
+    auto put = [&img](const void* src, size_t bytes) {
+        const size_t at = (img.size() + 15) / 16 * 16;
+        img.resize(at + bytes);
+        std::memcpy(img.data() + at, src, bytes);
+        return at;
+    };
+    std::vector<rtdbs_pool::Launch> plan;
+    std::vector<BatchItem> all_items;
+    for (int j = 0; j < maxchunks; ++j) {
+        std::vector<BatchItem> items;
+        for (int i = 0; i < n; ++i) {
+            const rtdbs_engine* e = p->eng[ids[i]];
+            const int S = e->p.stride, C = e->chunk;
+            if (j * C >= S) continue;
+            BatchItem it;
+            it.view = ids[i];
+            it.j = j;
+            it.c = std::min(C, S - j * C);
+            it.stg_off = j * C;
+            it.input = p->d_input + off[i];
+            items.push_back(it);
+        }
+        if (j == 0) all_items = items;
+        const size_t items_off = put(items.data(), sizeof(BatchItem) * items.size());
+        for (int ph = 0; ph < rtdbs::kBatchChunkPhases; ++ph) {
+            std::vector<int> prefix(items.size() + 1, 0);
+            int max_c = 0;
+            for (size_t i = 0; i < items.size(); ++i) {
+                prefix[i + 1] = prefix[i] + rtdbs::batch_blocks(ph, p->eng[items[i].view]->v, items[i].c);
+                max_c = std::max(max_c, items[i].c);
+            }
+            const size_t prefix_off = put(prefix.data(), sizeof(int) * prefix.size());
+            plan.push_back({ph, items_off, prefix_off, (int)items.size(), prefix.back(), max_c});
+        }
+    }
+    const size_t all_off = put(all_items.data(), sizeof(BatchItem) * all_items.size());
+    for (int ph = rtdbs::kBatchUnion; ph <= rtdbs::kBatchLabel; ++ph) {
+        std::vector<int> prefix(all_items.size() + 1, 0);
+        for (size_t i = 0; i < all_items.size(); ++i)
+            prefix[i + 1] = prefix[i] + rtdbs::batch_blocks(ph, p->eng[all_items[i].view]->v, 0);
+        const size_t prefix_off = put(prefix.data(), sizeof(int) * prefix.size());
+        plan.push_back({ph, all_off, prefix_off, (int)all_items.size(), prefix.back(), 0});
+    }
+    if (img.size() > p->tables_cap) {
+        if (p->d_tables) cudaFree(p->d_tables);
+        p->d_tables = nullptr;
+        CUDA_TRY(cudaMalloc((void**)&p->d_tables, img.size()));
+        p->tables_cap = img.size();
+    }
+    CUDA_TRY(cudaStreamSynchronize(p->stream));  // the tables may be in use by the last round
+    CUDA_TRY(cudaMemcpy(p->d_tables, img.data(), img.size(), cudaMemcpyHostToDevice));
+    p->plan = std::move(plan);
+    p->input_off = std::move(off);
+    p->input_floats = floats;
+    p->shape_ids = ids;
+    return RTDBS_OK;
+}
+
+int pool_enqueue_round(rtdbs_pool* p) {
+    for (const auto& l : p->plan) {
+        rtdbs::BatchLaunch L;
+        L.views = p->d_views;
+        L.items = reinterpret_cast<const rtdbs::BatchItem*>(p->d_tables + l.items_off);
+        L.prefix = reinterpret_cast<const int*>(p->d_tables + l.prefix_off);
+        L.n = l.n;
+        CUDA_TRY(rtdbs::launch_batch(l.phase, L, l.blocks, l.max_c, p->stream));
+    }
+    return RTDBS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rtdbs_pool_params_init(rtdbs_pool_params* pp) {
+    if (!pp) return fail(RTDBS_ERR_INVALID, "params is NULL");
+    std::memset(pp, 0, sizeof(*pp));
+    pp->max_streams = 1024;
+    return RTDBS_OK;
+}
+
+int rtdbs_pool_create(const rtdbs_pool_params* pp, void* cuda_stream, rtdbs_pool** out) {
+    if (!pp || !out) return fail(RTDBS_ERR_INVALID, "params/out is NULL");
+    *out = nullptr;
+    if (pp->max_streams <= 0 || pp->max_streams > (1 << 20)) return fail(RTDBS_ERR_INVALID, "bad max_streams");
+    if (pp->hbm_budget_bytes < 0) return fail(RTDBS_ERR_INVALID, "negative budget");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(RTDBS_ERR_NO_DEVICE, "no CUDA device available");
+    if (pp->device < 0 || pp->device >= ndev) return fail(RTDBS_ERR_INVALID, "device out of range");
+    DeviceGuard guard(pp->device);
+    CUDA_TRY(guard.err);
+    CUDA_TRY(configure_device(pp->device));
+    rtdbs_pool* p = new (std::nothrow) rtdbs_pool();
+    if (!p) return fail(RTDBS_ERR_OOM, "host allocation failed");
+    p->device = pp->device;
+    p->flags = pp->flags;
+    p->budget = pp->hbm_budget_bytes;
+    p->capacity = pp->max_streams;
+    p->eng.assign(p->capacity, nullptr);
+    p->loaded.assign(p->capacity, 0);
+    int rc = RTDBS_OK;
+    if (cuda_stream) {
+        p->stream = static_cast<cudaStream_t>(cuda_stream);
+    } else if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        rc = fail(RTDBS_ERR_CUDA, "cudaStreamCreate failed");
+    } else {
+        p->own_stream = true;
+    }
+    if (rc == RTDBS_OK && (cudaMalloc((void**)&p->d_views, sizeof(View) * p->capacity) != cudaSuccess ||
+                           cudaMalloc((void**)&p->d_ctls, sizeof(Ctl) * p->capacity) != cudaSuccess ||
+                           cudaMallocHost((void**)&p->h_ctls, sizeof(Ctl) * p->capacity) != cudaSuccess))
+        rc = fail(RTDBS_ERR_OOM, "pool tables: allocation failed");
+    if (rc == RTDBS_OK && cudaMemset(p->d_ctls, 0, sizeof(Ctl) * p->capacity) != cudaSuccess)
+        rc = fail(RTDBS_ERR_CUDA, "cudaMemset failed");
+    if (rc != RTDBS_OK) {
+        rtdbs_pool_destroy(p);
+        return rc;
+    }
+    *out = p;
+    return RTDBS_OK;
+}
+
+int rtdbs_pool_destroy(rtdbs_pool* p) {
+    if (!p) return RTDBS_OK;
+    DeviceGuard guard(p->device);
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    pool_drop_shape(p);
+    for (auto* e : p->eng)
+        if (e) rtdbs_destroy(e);
+    if (p->d_views) cudaFree(p->d_views);
+    if (p->d_ctls) cudaFree(p->d_ctls);
+    if (p->h_ctls) cudaFreeHost(p->h_ctls);
+    if (p->d_tables) cudaFree(p->d_tables);
+    if (p->d_input) cudaFree(p->d_input);
+    if (p->own_stream && p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+    return RTDBS_OK;
+}
+
+int rtdbs_pool_add_stream(rtdbs_pool* p, const rtdbs_params* params, int32_t* stream_id) {
+    if (!p || !params || !stream_id) return fail(RTDBS_ERR_INVALID, "pool/params/stream_id is NULL");
+    int64_t bytes = 0;
+    int rc = rtdbs_stream_bytes(params, &bytes);
+    if (rc != RTDBS_OK) return rc;
+    if (p->budget > 0 && p->used + bytes > p->budget)
+        return fail(RTDBS_ERR_BUDGET, "stream needs %lld bytes, %lld of %lld in use", (long long)bytes,
+                    (long long)p->used, (long long)p->budget);
+    int slot = -1;
+    for (int i = 0; i < p->capacity; ++i)
+        if (!p->eng[i]) {
+            slot = i;
+            break;
+        }
+    if (slot < 0) return fail(RTDBS_ERR_BUDGET, "all %d stream slots are in use", p->capacity);
+    rtdbs_params q = *params;
+    q.device = p->device;
+    q.flags |= RTDBS_FLAG_NO_GRAPH;
+    rtdbs_engine* e = nullptr;
+    rc = rtdbs_create(&q, p->stream, &e);
+    if (rc != RTDBS_OK) return rc;
+    // this stream's control block lives in the pool's contiguous array
+    e->v.ctl = p->d_ctls + slot;
+    {
+        DeviceGuard guard(p->device);
+        if (cudaMemsetAsync(e->v.ctl, 0, sizeof(Ctl), p->stream) != cudaSuccess) {
+            rtdbs_destroy(e);
+            return fail(RTDBS_ERR_CUDA, "cudaMemsetAsync failed");
+        }
+    }
+    p->eng[slot] = e;
+    p->loaded[slot] = 0;
+    p->used += (int64_t)e->dev_bytes;
+    *stream_id = slot;
+    return RTDBS_OK;
+}
+
+int rtdbs_pool_remove_stream(rtdbs_pool* p, int32_t id) {
+    if (!p || id < 0 || id >= p->capacity || !p->eng[id]) return fail(RTDBS_ERR_INVALID, "no such stream");
+    DeviceGuard guard(p->device);
+    cudaStreamSynchronize(p->stream);
+    for (int s : p->shape_ids)
+        if (s == id) {
+            pool_drop_shape(p);
+            break;
+        }
+    p->used -= (int64_t)p->eng[id]->dev_bytes;
+    rtdbs_destroy(p->eng[id]);
+    p->eng[id] = nullptr;
+    p->loaded[id] = 0;
+    return RTDBS_OK;
+}
+
+int rtdbs_pool_load_window(rtdbs_pool* p, int32_t id, const float* points, int points_on_device) {
+    if (!p || id < 0 || id >= p->capacity || !p->eng[id]) return fail(RTDBS_ERR_INVALID, "no such stream");
+    rtdbs_engine* e = p->eng[id];
+    int rc = rtdbs_load_window(e, points, points_on_device);
+    if (rc != RTDBS_OK) return rc;
+    DeviceGuard guard(p->device);
+    CUDA_TRY(cudaMemcpy(p->d_views + id, &e->v, sizeof(View), cudaMemcpyHostToDevice));
+    p->loaded[id] = 1;
+    for (int s : p->shape_ids)
+        if (s == id) {
+            pool_drop_shape(p);
+            break;
+        }
+    return RTDBS_OK;
+}
+
+int rtdbs_pool_slide(rtdbs_pool* p, int32_t n, const int32_t* ids, const float* d_points) {
+    if (!p || n <= 0 || !ids || !d_points) return fail(RTDBS_ERR_INVALID, "pool/ids/points is NULL or n <= 0");
+    std::vector<int> list(ids, ids + n);
+    std::vector<char> seen(p->capacity, 0);
+    for (int id : list) {
+        if (id < 0 || id >= p->capacity || !p->eng[id] || !p->loaded[id])
+            return fail(RTDBS_ERR_STATE, "stream %d is not loaded", id);
+        if (seen[id]) return fail(RTDBS_ERR_INVALID, "stream %d listed twice", id);
+        seen[id] = 1;
+    }
+    DeviceGuard guard(p->device);
+    CUDA_TRY(guard.err);
+    if (list != p->shape_ids) {
+        pool_drop_shape(p);
+        int rc = pool_build_shape(p, list);
+        if (rc != RTDBS_OK) return rc;
+    }
+    CUDA_TRY(cudaMemcpyAsync(p->d_input, d_points, sizeof(float) * p->input_floats, cudaMemcpyDeviceToDevice,
+                             p->stream));
+    if (p->flags & RTDBS_FLAG_NO_GRAPH) {
+        int rc = pool_enqueue_round(p);
+        if (rc != RTDBS_OK) return rc;
+    } else {
+        if (!p->graph) {
+            cudaGraph_t g = nullptr;
+            CUDA_TRY(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+            int rc = pool_enqueue_round(p);
+            cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
+            if (rc != RTDBS_OK) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            CUDA_TRY(ce);
+            cudaError_t ie = cudaGraphInstantiate(&p->graph, g, 0);
+            cudaGraphDestroy(g);
+            CUDA_TRY(ie);
+        } else {
+            ++p->graph_replays;
+        }
+        CUDA_TRY(cudaGraphLaunch(p->graph, p->stream));
+    }
+    ++p->rounds;
+    return RTDBS_OK;
+}
+
+int rtdbs_pool_sync(rtdbs_pool* p) {
+    if (!p) return fail(RTDBS_ERR_INVALID, "pool is NULL");
+    DeviceGuard guard(p->device);
+    CUDA_TRY(guard.err);
+    CUDA_TRY(cudaMemcpyAsync(p->h_ctls, p->d_ctls, sizeof(Ctl) * p->capacity, cudaMemcpyDeviceToHost, p->stream));
+    CUDA_TRY(cudaStreamSynchronize(p->stream));
+    for (int i = 0; i < p->capacity; ++i)
+        if (p->eng[i] && p->h_ctls[i].err)
+            return fail(RTDBS_ERR_DEVICE, "stream %d: device error bits 0x%x", i, p->h_ctls[i].err);
+    return RTDBS_OK;
+}
+
+int rtdbs_pool_outputs(rtdbs_pool* p, int32_t id, int32_t** d_label, int32_t** d_cluster_id) {
+    if (!p || id < 0 || id >= p->capacity || !p->eng[id]) return fail(RTDBS_ERR_INVALID, "no such stream");
+    return rtdbs_device_outputs(p->eng[id], d_label, d_cluster_id);
+}
+
+int rtdbs_pool_read_outputs(rtdbs_pool* p, int32_t id, int32_t* label, int32_t* cluster_id, int on_device) {
+    if (!p || id < 0 || id >= p->capacity || !p->eng[id]) return fail(RTDBS_ERR_INVALID, "no such stream");
+    DeviceGuard guard(p->device);
+    CUDA_TRY(guard.err);
+    int rc = copy_out(p->eng[id], label, cluster_id, on_device);
+    if (rc != RTDBS_OK) return rc;
+    CUDA_TRY(cudaStreamSynchronize(p->stream));
+    return RTDBS_OK;
+}
+
+int rtdbs_pool_engine(rtdbs_pool* p, int32_t id, rtdbs_engine** engine) {
+    if (!p || !engine || id < 0 || id >= p->capacity || !p->eng[id]) return fail(RTDBS_ERR_INVALID, "no such stream");
+    *engine = p->eng[id];
+    return RTDBS_OK;
+}
+
+int rtdbs_pool_get_stats(rtdbs_pool* p, rtdbs_pool_stats* s) {
+    if (!p || !s) return fail(RTDBS_ERR_INVALID, "pool/stats is NULL");
+    std::memset(s, 0, sizeof(*s));
+    for (int i = 0; i < p->capacity; ++i) s->streams += p->eng[i] ? 1 : 0;
+    s->bytes_in_use = p->used;
+    s->budget_bytes = p->budget;
+    s->rounds = p->rounds;
+    s->graph_replays = p->graph_replays;
+    s->launches_per_round = (int32_t)p->plan.size();
+    return RTDBS_OK;
 }
 
 }  // extern "C"

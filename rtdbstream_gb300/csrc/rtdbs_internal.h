@@ -82,6 +82,7 @@ struct View {
     int key_bits;
     int sort_passes;
     int max_items;
+    int precision;              // RTDBS_PREC_* (batched launches dispatch on it)
     // buffers
     float4* ring;
     unsigned long long* kslot;
@@ -129,5 +130,45 @@ cudaError_t launch_chunk_step(const View& v, int precision, int j, int c, int in
 cudaError_t launch_cluster(const View& v, int precision, int advance, cudaStream_t s);
 cudaError_t launch_counts_by_slot(const View& v, int* nn_by_slot, cudaStream_t s);
 cudaError_t configure_kernels();
+
+// ------------------------------------------------------------ batched launches
+// One launch of a phase covers many streams: block b belongs to the item i
+// with prefix[i] <= b < prefix[i+1] and runs that stream's kernel body with
+// block index b - prefix[i] of prefix[i+1] - prefix[i].
+
+enum BatchPhase : int {
+    kBatchIngest = 0,
+    kBatchSort,
+    kBatchRunmerge,
+    kBatchDecrement,
+    kBatchMerge,
+    kBatchBuild,
+    kBatchIncrement,
+    kBatchUnion,
+    kBatchFlatten,
+    kBatchLabel,
+    kNumBatchPhases
+};
+constexpr int kBatchChunkPhases = 7;  // ingest .. increment
+
+struct BatchItem {
+    int view;            // index into the View array
+    int j;               // chunk index within the slide
+    int c;               // points in the chunk
+    int stg_off;         // offset of the chunk within the stream's new points
+    const float* input;  // the stream's new points of this slide (device)
+};
+
+struct BatchLaunch {
+    const View* views;
+    const BatchItem* items;
+    const int* prefix;   // n + 1 entries
+    int n;
+};
+
+// Blocks one item needs in a phase (same shapes as the single-stream launches).
+int batch_blocks(int phase, const View& v, int c);
+int batch_threads(int phase);
+cudaError_t launch_batch(int phase, const BatchLaunch& L, int total_blocks, int max_c, cudaStream_t s);
 
 }  // namespace rtdbs

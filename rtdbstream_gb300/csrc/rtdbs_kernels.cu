@@ -314,16 +314,17 @@ __device__ __forceinline__ void flush_stats(const View& v, unsigned rechecks, in
 
 // New points of chunk j -> ring slots [el, el+c): float4 + cell key; the
 // points they replace are kept for the decrement pass.
-__global__ void k_ingest(View v, int j, int c, int init, int stg_off) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) v.ctl->b += 1;  // no reader in this kernel
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void ingest_body(const View& v, int j, int c, int init, int stg_off,
+                                            const float* input, int bx) {
+    if (bx == 0 && threadIdx.x == 0) v.ctl->b += 1;  // no reader in this kernel
+    const int k = bx * blockDim.x + threadIdx.x;
     if (k >= c) return;
     const int slot = chunk_base_slot(v, j, init) + k;
     if (!init) {
         v.xpt[k] = v.ring[slot];
         v.xsort[k] = (v.kslot[slot] << kOffBits) | (unsigned long long)k;
     }
-    const float* p = v.staging + (size_t)(stg_off + k) * v.dim;
+    const float* p = input + (size_t)(stg_off + k) * v.dim;
     const float x = p[0];
     const float y = v.dim > 1 ? p[1] : 0.0f;
     const float z = v.dim > 2 ? p[2] : 0.0f;
@@ -331,6 +332,10 @@ __global__ void k_ingest(View v, int j, int c, int init, int stg_off) {
     const unsigned long long key = cell_key(v, x, y, z);
     v.kslot[slot] = key;
     v.nsort[k] = (key << kOffBits) | (unsigned long long)k;
+}
+
+__global__ void k_ingest(View v, int j, int c, int init, int stg_off) {
+    ingest_body(v, j, c, init, stg_off, v.staging, blockIdx.x);
 }
 
 // Exclusive scan of one value per thread over a 1024-thread block.
@@ -367,13 +372,19 @@ __device__ __forceinline__ unsigned block_excl_scan_1024(unsigned val, unsigned*
 // eight ballots; per-(digit, warp) counters are scanned in digit-major order
 // so the order of equal digits is the item order.  The merge consumes the
 // sorted runs directly.
-__global__ void __launch_bounds__(kSortRun) k_sort(View v, int c, int init) {
-    __shared__ unsigned long long buf[kSortRun];
-    __shared__ unsigned whist[256 * 32];
-    __shared__ unsigned wsum[32];
-    const int which = blockIdx.y;
+struct SortSmem {
+    unsigned long long buf[kSortRun];
+    unsigned whist[256 * 32];
+    unsigned wsum[32];
+};
+
+__device__ __forceinline__ void sort_body(const View& v, int c, int init, int bx, int by, SortSmem& sm) {
+    unsigned long long* buf = sm.buf;
+    unsigned* whist = sm.whist;
+    unsigned* wsum = sm.wsum;
+    const int which = by;
     if (which == 1 && init) return;
-    const int r0 = blockIdx.x * kSortRun;
+    const int r0 = bx * kSortRun;
     const int len = min(kSortRun, c - r0);
     if (len <= 0) return;
     unsigned long long* run = (which ? v.xsort : v.nsort) + r0;  // sorted in place
@@ -416,20 +427,25 @@ __global__ void __launch_bounds__(kSortRun) k_sort(View v, int c, int init) {
     if (tid < len) run[tid] = it;
 }
 
+__global__ void __launch_bounds__(kSortRun) k_sort(View v, int c, int init) {
+    __shared__ SortSmem sm;
+    sort_body(v, c, init, blockIdx.x, blockIdx.y, sm);
+}
+
 // Merges the sorted runs of kSortRun words into one sorted list: a word's
 // rank is its index in its run plus the words below it in every other run
 // (words are distinct, so ranks are too).  Block (r, y) ranks run r of the
 // new (y = 0) or expired (y = 1) words; all c words are staged in shared
 // memory first, so the binary searches stay on chip.
-__global__ void __launch_bounds__(kSortRun) k_runmerge(View v, int c, int init) {
-    extern __shared__ unsigned long long words[];
-    const int which = blockIdx.y;
+__device__ __forceinline__ void runmerge_body(const View& v, int c, int init, int bx, int by,
+                                              unsigned long long* words) {
+    const int which = by;
     if (which == 1 && init) return;
     const unsigned long long* runs = which ? v.xsort : v.nsort;
     unsigned long long* out = which ? v.xword : v.nword;
     for (int i = threadIdx.x; i < c; i += blockDim.x) words[i] = runs[i];
     __syncthreads();
-    const int own = blockIdx.x;
+    const int own = bx;
     const int i = own * kSortRun + threadIdx.x;
     if (i >= c) return;
     const unsigned long long w = words[i];
@@ -451,12 +467,22 @@ __global__ void __launch_bounds__(kSortRun) k_runmerge(View v, int c, int init) 
     out[rank] = w;
 }
 
+__global__ void __launch_bounds__(kSortRun) k_runmerge(View v, int c, int init) {
+    extern __shared__ unsigned long long words[];
+    runmerge_body(v, c, init, blockIdx.x, blockIdx.y, words);
+}
+
 // -1 on the count of every surviving neighbour of each expired point (old grid).
+struct StreamSmem {
+    int rstart[8][9], rpre[8][10];
+};
+
 template <int MODE, int DIM>
-__global__ void __launch_bounds__(256) k_decr(View v, int j, int c) {
-    __shared__ int rstart[8][9], rpre[8][10];
+__device__ __forceinline__ void decr_body(const View& v, int j, int c, int bx, StreamSmem& sm) {
+    int(&rstart)[8][9] = sm.rstart;
+    int(&rpre)[8][10] = sm.rpre;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int gw = (bx * blockDim.x + threadIdx.x) >> 5;
     if (gw >= c) return;
     const long long b = v.ctl->b;
     const int old = (int)((b - 1) & 1);
@@ -479,6 +505,12 @@ __global__ void __launch_bounds__(256) k_decr(View v, int j, int c) {
         if ((qs < el || qs >= el + c) && is_nbr<MODE, DIM>(v, xp, q, rechecks)) atomicSub(&scnt[pos], 1);
     }
     flush_stats(v, rechecks, 0, lane);
+}
+
+template <int MODE, int DIM>
+__global__ void __launch_bounds__(256) k_decr(View v, int j, int c) {
+    __shared__ StreamSmem sm;
+    decr_body<MODE, DIM>(v, j, c, blockIdx.x, sm);
 }
 
 __device__ __forceinline__ bool tuple_less(unsigned long long ka, int sa, unsigned long long kb,
@@ -504,18 +536,26 @@ __device__ __forceinline__ int count_words_less(const unsigned long long* words,
 // Old sorted window minus the expired slots [el, el+c), merged with the c
 // new entries; tile t of the old window goes to output offset
 // ts - (#expired before ts) + (#new before old[ts]).
-__global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, int init) {
-    __shared__ unsigned long long tkey[kMergeTile];
-    __shared__ int tslot[kMergeTile];
-    __shared__ int spre[kMergeTile + 1];
-    __shared__ unsigned wsum[32];
+struct MergeSmem {
+    unsigned long long tkey[kMergeTile];
+    int tslot[kMergeTile];
+    int spre[kMergeTile + 1];
+    unsigned wsum[32];
+};
+
+__device__ __forceinline__ void merge_body(const View& v, int j, int c, int init, int bx, int nbx,
+                                           MergeSmem& sm) {
+    unsigned long long* tkey = sm.tkey;
+    int* tslot = sm.tslot;
+    int* spre = sm.spre;
+    unsigned* wsum = sm.wsum;
     const long long b = v.ctl->b;
     const int src = (int)((b - 1) & 1), dst = (int)(b & 1);
     const int n_old = v.ctl->nocc[src];
     const int n_new = n_old - (init ? 0 : c) + c;
     const int el = chunk_base_slot(v, j, init);
     const int tid = threadIdx.x;
-    if (blockIdx.x == 0 && tid == 0) {
+    if (bx == 0 && tid == 0) {
         v.ctl->nocc[dst] = n_new;
         v.ctl->nitems = 0;
         v.ctl->ncells = 0;
@@ -525,11 +565,11 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
     // Table generations wrap every kGenMod builds of a table: clear it then.
     if (b >= 2 && ((b >> 1) % (long long)kGenMod) == 0) {
         ulonglong2* T = v.table[dst];
-        for (unsigned i = blockIdx.x * blockDim.x + tid; i <= v.pmask; i += gridDim.x * blockDim.x)
+        for (unsigned i = bx * blockDim.x + tid; i <= v.pmask; i += nbx * blockDim.x)
             T[i] = make_ulonglong2(0ull, 0ull);
     }
     const int ntiles = n_old > 0 ? (n_old + kMergeTile - 1) / kMergeTile : 1;
-    const int t = blockIdx.x;
+    const int t = bx;
     if (t >= ntiles) return;
     const int ts = t * kMergeTile;
     const int te = min(ts + kMergeTile, n_old);
@@ -640,15 +680,26 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, i
     }
 }
 
+__global__ void __launch_bounds__(kMergeThreads) k_merge(View v, int j, int c, int init) {
+    __shared__ MergeSmem sm;
+    merge_body(v, j, c, init, blockIdx.x, gridDim.x, sm);
+}
+
 // Cell table and work list of the new sorted window.  A work item is a
 // maximal run of one cell inside a 32-aligned block of sorted positions.
 // Item and cell counters are reserved once per block.
-__global__ void __launch_bounds__(kBuildThreads) k_build(View v) {
-    __shared__ int wcount[kBuildThreads / 32];
-    __shared__ int wbase[kBuildThreads / 32];
-    __shared__ int bcells;
+struct BuildSmem {
+    int wcount[kBuildThreads / 32];
+    int wbase[kBuildThreads / 32];
+    int bcells;
+};
+
+__device__ __forceinline__ void build_body(const View& v, int bx, BuildSmem& sm) {
+    int* wcount = sm.wcount;
+    int* wbase = sm.wbase;
+    int& bcells = sm.bcells;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int gw = (bx * blockDim.x + threadIdx.x) >> 5;
     const long long b = v.ctl->b;
     const int cur = (int)(b & 1);
     const unsigned gen = gen_of_build(b);
@@ -699,12 +750,18 @@ __global__ void __launch_bounds__(kBuildThreads) k_build(View v) {
     if (err) atomicOr(&v.ctl->err, err);
 }
 
+__global__ void __launch_bounds__(kBuildThreads) k_build(View v) {
+    __shared__ BuildSmem sm;
+    build_body(v, blockIdx.x, sm);
+}
+
 // Full count of each new point and +1 on every older neighbour (new grid).
 template <int MODE, int DIM>
-__global__ void __launch_bounds__(256) k_incr(View v, int j, int c, int init) {
-    __shared__ int rstart[8][9], rpre[8][10];
+__device__ __forceinline__ void incr_body(const View& v, int j, int c, int init, int bx, StreamSmem& sm) {
+    int(&rstart)[8][9] = sm.rstart;
+    int(&rpre)[8][10] = sm.rpre;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int gw = (bx * blockDim.x + threadIdx.x) >> 5;
     if (gw >= c) return;
     const long long b = v.ctl->b;
     const int cur = (int)(b & 1);
@@ -746,6 +803,12 @@ __global__ void __launch_bounds__(256) k_incr(View v, int j, int c, int init) {
     flush_stats(v, rechecks, err, lane);
 }
 
+template <int MODE, int DIM>
+__global__ void __launch_bounds__(256) k_incr(View v, int j, int c, int init) {
+    __shared__ StreamSmem sm;
+    incr_body<MODE, DIM>(v, j, c, init, blockIdx.x, sm);
+}
+
 // Union of every core-core neighbour pair, each unordered pair once (the
 // candidate's sorted position is above the home point's).  A candidate's
 // root is found once per candidate chunk and compared with cached roots of
@@ -754,13 +817,19 @@ __global__ void __launch_bounds__(256) k_incr(View v, int j, int c, int init) {
 // from per-position root hints.  Each warp walks
 // a contiguous range of work items (neighbouring cells), so candidate loads
 // reuse L1.
+struct ClusterSmem {
+    int home_root[kClusterThreads / 32][32];
+    float4 home_pt[kClusterThreads / 32][32];
+    int rstart[kClusterThreads / 32][9], rpre[kClusterThreads / 32][10];
+};
+
 template <int MODE, int DIM>
-__global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
-    __shared__ int home_root[kClusterThreads / 32][32];
-    __shared__ float4 home_pt[kClusterThreads / 32][32];
-    __shared__ int rstart[kClusterThreads / 32][9], rpre[kClusterThreads / 32][10];
+__device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
+    float4(&home_pt)[kClusterThreads / 32][32] = sm.home_pt;
+    int(&rstart)[kClusterThreads / 32][9] = sm.rstart;
+    int(&rpre)[kClusterThreads / 32][10] = sm.rpre;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    volatile int* rh = home_root[wib];
+    volatile int* rh = sm.home_root[wib];
     const float4* hpt = home_pt[wib];
     const long long b = v.ctl->b;
     const int cur = (int)(b & 1);
@@ -851,23 +920,32 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
     flush_stats(v, rechecks, err, lane);
 }
 
+template <int MODE, int DIM>
+__global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
+    __shared__ ClusterSmem sm;
+    union_body<MODE, DIM>(v, sm);
+}
+
 // Root of every core point by sorted position (-1 for non-core points),
 // walked from the position's root hint.
-__global__ void k_flatten(View v) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) v.ctl->label_next = 0;  // k_label's queue; not read here
+__device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx) {
+    if (bx == 0 && threadIdx.x == 0) v.ctl->label_next = 0;  // k_label's queue; not read here
     const int cur = (int)(v.ctl->b & 1);
     const int n = v.ctl->nocc[cur];
     const int* scnt = v.scnt[cur];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (int i = bx * blockDim.x + threadIdx.x; i < n; i += nbx * blockDim.x)
         v.sroot[i] = scnt[i] >= v.min_pts ? uf_find(v.parent, v.sroot[i]) : -1;
 }
+
+__global__ void k_flatten(View v) { flatten_body(v, blockIdx.x, gridDim.x); }
 
 // Labels and ids by slot: core -> 0 and its root; non-core -> 1 and the
 // minimum root over adjacent cores, or 2 and its own slot.
 template <int MODE, int DIM>
-__global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advance) {
-    __shared__ int rstart[kClusterThreads / 32][9], rpre[kClusterThreads / 32][10];
-    __shared__ float4 home_pt[kClusterThreads / 32][32];
+__device__ __forceinline__ void label_body(const View& v, int advance, int bx, ClusterSmem& sm) {
+    int(&rstart)[kClusterThreads / 32][9] = sm.rstart;
+    int(&rpre)[kClusterThreads / 32][10] = sm.rpre;
+    float4(&home_pt)[kClusterThreads / 32][32] = sm.home_pt;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const float4* hpt = home_pt[wib];
     const long long b = v.ctl->b;
@@ -940,10 +1018,16 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advanc
         }
     }
     flush_stats(v, rechecks, 0, lane);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (bx == 0 && threadIdx.x == 0) {
         v.ctl->union_next = 0;                // the next clustering's queue; not read here
         if (advance) v.ctl->slide += 1;       // no reader here
     }
+}
+
+template <int MODE, int DIM>
+__global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advance) {
+    __shared__ ClusterSmem sm;
+    label_body<MODE, DIM>(v, advance, blockIdx.x, sm);
 }
 
 __global__ void k_counts_by_slot(View v, int* nn) {
@@ -954,6 +1038,97 @@ __global__ void k_counts_by_slot(View v, int* nn) {
 }
 
 int g_num_sms = 0;
+// ------------------------------------------------------------- batched kernel
+
+#define RTDBS_BODY_DISPATCH(prec, dim, BODY, ...)                                 \
+    do {                                                                           \
+        if ((prec) == kPrecFp32) {                                                 \
+            if ((dim) == 1) BODY<kPrecFp32, 1>(__VA_ARGS__);                       \
+            else if ((dim) == 2) BODY<kPrecFp32, 2>(__VA_ARGS__);                  \
+            else BODY<kPrecFp32, 3>(__VA_ARGS__);                                  \
+        } else {                                                                   \
+            if ((dim) == 1) BODY<kPrecFp64, 1>(__VA_ARGS__);                       \
+            else if ((dim) == 2) BODY<kPrecFp64, 2>(__VA_ARGS__);                  \
+            else BODY<kPrecFp64, 3>(__VA_ARGS__);                                  \
+        }                                                                          \
+    } while (0)
+
+template <int PHASE>
+struct PhaseShape;
+template <> struct PhaseShape<kBatchIngest> { static constexpr int threads = 256, min_blocks = 1; };
+template <> struct PhaseShape<kBatchSort> { static constexpr int threads = kSortRun, min_blocks = 1; };
+template <> struct PhaseShape<kBatchRunmerge> { static constexpr int threads = kSortRun, min_blocks = 1; };
+template <> struct PhaseShape<kBatchDecrement> { static constexpr int threads = 256, min_blocks = 1; };
+template <> struct PhaseShape<kBatchMerge> { static constexpr int threads = kMergeThreads, min_blocks = 1; };
+template <> struct PhaseShape<kBatchBuild> { static constexpr int threads = kBuildThreads, min_blocks = 1; };
+template <> struct PhaseShape<kBatchIncrement> { static constexpr int threads = 256, min_blocks = 1; };
+template <> struct PhaseShape<kBatchUnion> { static constexpr int threads = kClusterThreads, min_blocks = 6; };
+template <> struct PhaseShape<kBatchFlatten> { static constexpr int threads = 256, min_blocks = 1; };
+template <> struct PhaseShape<kBatchLabel> { static constexpr int threads = kClusterThreads, min_blocks = 6; };
+
+// One phase over many streams.  The block finds its item, copies that
+// stream's View into shared memory and runs the stream's kernel body.
+template <int PHASE>
+__global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>::min_blocks)
+    k_batch(BatchLaunch L) {
+    __shared__ View sv;
+    __shared__ int s_item, s_bx, s_nbx;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = L.n;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (L.prefix[mid] <= (int)blockIdx.x)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        s_item = lo;
+        s_bx = (int)blockIdx.x - L.prefix[lo];
+        s_nbx = L.prefix[lo + 1] - L.prefix[lo];
+    }
+    __syncthreads();
+    const BatchItem it = L.items[s_item];
+    {
+        const int* src = reinterpret_cast<const int*>(L.views + it.view);
+        int* dst = reinterpret_cast<int*>(&sv);
+        for (int i = threadIdx.x; i < (int)(sizeof(View) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const int bx = s_bx, nbx = s_nbx;
+    const int prec = sv.precision, dim = sv.dim;
+    if constexpr (PHASE == kBatchIngest) {
+        ingest_body(sv, it.j, it.c, 0, it.stg_off, it.input, bx);
+    } else if constexpr (PHASE == kBatchSort) {
+        __shared__ SortSmem sm;
+        const int nruns = (it.c + kSortRun - 1) / kSortRun;
+        sort_body(sv, it.c, 0, bx % nruns, bx / nruns, sm);
+    } else if constexpr (PHASE == kBatchRunmerge) {
+        extern __shared__ unsigned long long words[];
+        const int nruns = (it.c + kSortRun - 1) / kSortRun;
+        runmerge_body(sv, it.c, 0, bx % nruns, bx / nruns, words);
+    } else if constexpr (PHASE == kBatchDecrement) {
+        __shared__ StreamSmem sm;
+        RTDBS_BODY_DISPATCH(prec, dim, decr_body, sv, it.j, it.c, bx, sm);
+    } else if constexpr (PHASE == kBatchMerge) {
+        __shared__ MergeSmem sm;
+        merge_body(sv, it.j, it.c, 0, bx, nbx, sm);
+    } else if constexpr (PHASE == kBatchBuild) {
+        __shared__ BuildSmem sm;
+        build_body(sv, bx, sm);
+    } else if constexpr (PHASE == kBatchIncrement) {
+        __shared__ StreamSmem sm;
+        RTDBS_BODY_DISPATCH(prec, dim, incr_body, sv, it.j, it.c, 0, bx, sm);
+    } else if constexpr (PHASE == kBatchUnion) {
+        __shared__ ClusterSmem sm;
+        RTDBS_BODY_DISPATCH(prec, dim, union_body, sv, sm);
+    } else if constexpr (PHASE == kBatchFlatten) {
+        flatten_body(sv, bx, nbx);
+    } else {
+        __shared__ ClusterSmem sm;
+        RTDBS_BODY_DISPATCH(prec, dim, label_body, sv, 1, bx, sm);
+    }
+}
+
 std::atomic<unsigned long long> g_runmerge_ready{0};  // one bit per device
 
 // k_runmerge stages up to kChunkMax words (128 KB) in dynamic shared memory;
@@ -963,8 +1138,10 @@ void ensure_runmerge_smem() {
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
     const unsigned long long bit = 1ull << dev;
     if (g_runmerge_ready.load() & bit) return;
-    if (cudaFuncSetAttribute(k_runmerge, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)(sizeof(unsigned long long) * kChunkMax)) == cudaSuccess)
+    const int bytes = (int)(sizeof(unsigned long long) * kChunkMax);
+    if (cudaFuncSetAttribute(k_runmerge, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess &&
+        cudaFuncSetAttribute(k_batch<kBatchRunmerge>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) ==
+            cudaSuccess)
         g_runmerge_ready.fetch_or(bit);
 }
 
@@ -1056,6 +1233,57 @@ cudaError_t launch_cluster(const View& v, int precision, int advance, cudaStream
     for (int ph = kPhaseUnion; ph <= kPhaseLabel && e == cudaSuccess; ++ph)
         e = launch_phase(ph, v, precision, 0, 0, 0, 0, advance, s);
     return e;
+}
+
+int batch_threads(int phase) {
+    switch (phase) {
+        case kBatchSort:
+        case kBatchRunmerge: return kSortRun;
+        case kBatchMerge: return kMergeThreads;
+        case kBatchBuild: return kBuildThreads;
+        case kBatchUnion:
+        case kBatchLabel: return kClusterThreads;
+        default: return 256;
+    }
+}
+
+int batch_blocks(int phase, const View& v, int c) {
+    const int runs = (c + kSortRun - 1) / kSortRun;
+    switch (phase) {
+        case kBatchIngest: return (c + 255) / 256;
+        case kBatchSort:
+        case kBatchRunmerge: return 2 * runs;
+        case kBatchDecrement:
+        case kBatchIncrement: return (c * 32 + 255) / 256;
+        case kBatchMerge: return (v.W + kMergeTile - 1) / kMergeTile;
+        case kBatchBuild: return (v.W + kBuildThreads - 1) / kBuildThreads;
+        case kBatchUnion:
+        case kBatchLabel: return max(1, min(1024, (v.W + 4095) / 4096));  // persistent, queue-fed
+        case kBatchFlatten: return max(1, min(1024, (v.W + 2047) / 2048));
+        default: return 0;
+    }
+}
+
+cudaError_t launch_batch(int phase, const BatchLaunch& L, int total_blocks, int max_c, cudaStream_t s) {
+    if (total_blocks <= 0 || L.n <= 0) return cudaSuccess;
+    const int t = batch_threads(phase);
+    switch (phase) {
+        case kBatchIngest: k_batch<kBatchIngest><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchSort: k_batch<kBatchSort><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchRunmerge:
+            ensure_runmerge_smem();
+            k_batch<kBatchRunmerge><<<total_blocks, t, sizeof(unsigned long long) * max_c, s>>>(L);
+            break;
+        case kBatchDecrement: k_batch<kBatchDecrement><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchMerge: k_batch<kBatchMerge><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchBuild: k_batch<kBatchBuild><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchIncrement: k_batch<kBatchIncrement><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchUnion: k_batch<kBatchUnion><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchFlatten: k_batch<kBatchFlatten><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchLabel: k_batch<kBatchLabel><<<total_blocks, t, 0, s>>>(L); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_counts_by_slot(const View& v, int* nn, cudaStream_t s) {

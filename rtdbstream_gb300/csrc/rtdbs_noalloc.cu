@@ -166,6 +166,7 @@ extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int
     v.units = 1;
     v.min_pts = min_pts;
     v.chunk = n;
+    v.precision = precision;
     const double E = eps * eps, m = 1.0 / 1048576.0;
     float flo = (float)(E * (1.0 - m)), fhi = (float)(E * (1.0 + m));
     if ((double)flo > E * (1.0 - m)) flo = std::nextafter(flo, 0.0f);

@@ -32,7 +32,12 @@ EXPORTED_SYMBOLS = (
     "rtdbs_create", "rtdbs_destroy", "rtdbs_load_window", "rtdbs_slide", "rtdbs_slide_async",
     "rtdbs_sync", "rtdbs_cluster", "rtdbs_get_counts", "rtdbs_device_outputs", "rtdbs_get_stats",
     "rtdbs_slide_profiled", "rtdbs_cluster_window_noalloc",
+    "rtdbs_stream_bytes", "rtdbs_pool_params_init", "rtdbs_pool_create", "rtdbs_pool_destroy",
+    "rtdbs_pool_add_stream", "rtdbs_pool_remove_stream", "rtdbs_pool_load_window", "rtdbs_pool_slide",
+    "rtdbs_pool_sync", "rtdbs_pool_outputs", "rtdbs_pool_read_outputs", "rtdbs_pool_engine",
+    "rtdbs_pool_get_stats",
 )
+RTDBS_ERR_BUDGET = -7
 
 
 class Params(ctypes.Structure):
@@ -58,6 +63,19 @@ PHASES = ("ingest", "sort", "decrement", "merge", "build", "increment", "union",
 class PhaseTimes(ctypes.Structure):
     _fields_ = [(f"{p}_ms", ctypes.c_float) for p in PHASES] + [
         ("total_ms", ctypes.c_float), ("chunks", ctypes.c_int32)]
+
+
+class PoolParams(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("flags", ctypes.c_int32), ("max_streams", ctypes.c_int32),
+                ("reserved0", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64),
+                ("reserved", ctypes.c_int64 * 6)]
+
+
+class PoolStats(ctypes.Structure):
+    _fields_ = [("streams", ctypes.c_int64), ("bytes_in_use", ctypes.c_int64), ("budget_bytes", ctypes.c_int64),
+                ("rounds", ctypes.c_int64), ("graph_replays", ctypes.c_int64),
+                ("launches_per_round", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+                ("reserved", ctypes.c_int64 * 4)]
 
 
 class RtdbsError(RuntimeError):
@@ -96,6 +114,19 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     L.rtdbs_device_outputs.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
     L.rtdbs_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     L.rtdbs_slide_profiled.argtypes = [vp, vp, ctypes.POINTER(PhaseTimes)]
+    L.rtdbs_stream_bytes.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(ctypes.c_int64)]
+    L.rtdbs_pool_params_init.argtypes = [ctypes.POINTER(PoolParams)]
+    L.rtdbs_pool_create.argtypes = [ctypes.POINTER(PoolParams), vp, ctypes.POINTER(vp)]
+    L.rtdbs_pool_destroy.argtypes = [vp]
+    L.rtdbs_pool_add_stream.argtypes = [vp, ctypes.POINTER(Params), ctypes.POINTER(ctypes.c_int32)]
+    L.rtdbs_pool_remove_stream.argtypes = [vp, ctypes.c_int32]
+    L.rtdbs_pool_load_window.argtypes = [vp, ctypes.c_int32, vp, ctypes.c_int]
+    L.rtdbs_pool_slide.argtypes = [vp, ctypes.c_int32, vp, vp]
+    L.rtdbs_pool_sync.argtypes = [vp]
+    L.rtdbs_pool_outputs.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    L.rtdbs_pool_read_outputs.argtypes = [vp, ctypes.c_int32, vp, vp, ctypes.c_int]
+    L.rtdbs_pool_engine.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(vp)]
+    L.rtdbs_pool_get_stats.argtypes = [vp, ctypes.POINTER(PoolStats)]
     for name in EXPORTED_SYMBOLS:
         getattr(L, name).restype = getattr(L, name).restype or ctypes.c_int
     _lib = L
@@ -227,3 +258,109 @@ class Engine:
         s = Stats()
         _check(self._lib.rtdbs_get_stats(self._h, ctypes.byref(s)))
         return {f: getattr(s, f) for f, _ in Stats._fields_ if f != "reserved"}
+
+
+def make_params(dim: int, window_size: int, stride_size: int, radius: float, min_pts: int,
+                precision: str = "fp64", bbox: Optional[Tuple] = None, device: int = 0,
+                use_graph: bool = True) -> Params:
+    L = load_library()
+    p = Params()
+    _check(L.rtdbs_params_init(ctypes.byref(p)))
+    p.dim, p.window, p.stride = int(dim), int(window_size), int(stride_size)
+    p.min_pts, p.eps = int(min_pts), float(radius)
+    p.precision = {"fp64": PREC_FP64, "fp32": PREC_FP32}[precision]
+    p.device = int(device)
+    p.flags = 0 if use_graph else FLAG_NO_GRAPH
+    if bbox is not None:
+        lo, hi = bbox
+        p.has_bbox = 1
+        for a in range(int(dim)):
+            p.bbox_min[a] = float(lo[a])
+            p.bbox_max[a] = float(hi[a])
+    return p
+
+
+def stream_bytes(params: Params) -> int:
+    """Device bytes one stream occupies (a pool's admission cost); no GPU needed."""
+    b = ctypes.c_int64()
+    _check(load_library().rtdbs_stream_bytes(ctypes.byref(params), ctypes.byref(b)))
+    return b.value
+
+
+class Pool:
+    """Many independent streams slid together, one launch per kernel phase."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, max_streams: int = 1024,
+                 use_graph: bool = True, stream: int = 0):
+        self._lib = load_library()
+        pp = PoolParams()
+        _check(self._lib.rtdbs_pool_params_init(ctypes.byref(pp)))
+        pp.device, pp.max_streams = int(device), int(max_streams)
+        pp.hbm_budget_bytes = int(hbm_budget_bytes)
+        pp.flags = 0 if use_graph else FLAG_NO_GRAPH
+        h = ctypes.c_void_p()
+        _check(self._lib.rtdbs_pool_create(ctypes.byref(pp), ctypes.c_void_p(stream), ctypes.byref(h)))
+        self._h = h
+        self.windows = {}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.rtdbs_pool_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def add_stream(self, params: Params) -> int:
+        sid = ctypes.c_int32()
+        _check(self._lib.rtdbs_pool_add_stream(self._h, ctypes.byref(params), ctypes.byref(sid)))
+        self.windows[sid.value] = (params.window, params.stride, params.dim)
+        return sid.value
+
+    def remove_stream(self, sid: int) -> None:
+        _check(self._lib.rtdbs_pool_remove_stream(self._h, int(sid)))
+        self.windows.pop(sid, None)
+
+    def load_window(self, sid: int, points) -> None:
+        if isinstance(points, np.ndarray):
+            a = np.ascontiguousarray(points, np.float32)
+            _check(self._lib.rtdbs_pool_load_window(self._h, int(sid), a.ctypes.data, 0))
+        else:
+            _check(self._lib.rtdbs_pool_load_window(self._h, int(sid), _ptr(points), 1))
+
+    def slide(self, sids, d_points) -> None:
+        """One round: streams `sids` slide; d_points is a device tensor holding
+        their new points back to back in that order."""
+        ids = (ctypes.c_int32 * len(sids))(*[int(x) for x in sids])
+        _check(self._lib.rtdbs_pool_slide(self._h, len(sids), ids, _ptr(d_points)))
+
+    def sync(self) -> None:
+        _check(self._lib.rtdbs_pool_sync(self._h))
+
+    def outputs(self, sid: int):
+        W = self.windows[sid][0]
+        lab = np.empty(W, np.int32)
+        cid = np.empty(W, np.int32)
+        _check(self._lib.rtdbs_pool_read_outputs(self._h, int(sid), lab.ctypes.data, cid.ctypes.data, 0))
+        return lab, cid
+
+    def counts(self, sid: int) -> np.ndarray:
+        e = ctypes.c_void_p()
+        _check(self._lib.rtdbs_pool_engine(self._h, int(sid), ctypes.byref(e)))
+        nn = np.empty(self.windows[sid][0], np.int32)
+        _check(self._lib.rtdbs_get_counts(e, nn.ctypes.data, 0))
+        return nn
+
+    def stats(self) -> dict:
+        s = PoolStats()
+        _check(self._lib.rtdbs_pool_get_stats(self._h, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in PoolStats._fields_ if not f.startswith("reserved")}

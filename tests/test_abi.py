@@ -90,3 +90,12 @@ def test_engine_raises_without_device():
         pytest.skip("a GPU is present")
     with pytest.raises(E.RtdbsError):
         E.Engine(2, 100, 10, 0.5, 4)
+
+
+def test_stream_bytes_without_device():
+    small = E.make_params(2, 1_000, 100, 0.5, 4)
+    big = E.make_params(3, 1_000_000, 10_000, 3.3e-3, 10)
+    a, b = E.stream_bytes(small), E.stream_bytes(big)
+    assert 0 < a < b
+    # dominated by the window-sized buffers: ~165 bytes per slot at W = 1M
+    assert 120 * 1_000_000 < b < 220 * 1_000_000
