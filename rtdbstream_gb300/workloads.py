@@ -150,3 +150,63 @@ def walker_eps(target: float = 20.0, seed: int = 1, iters: int = 24) -> float:
         else:
             hi = mid
     return float(np.sqrt(lo * hi))
+
+
+# ------------------------------------------------------------- stream mixes
+
+@dataclass(frozen=True)
+class MixStream:
+    dim: int
+    window: int
+    stride: int
+    eps: float
+    min_pts: int
+    seed: int
+    box: float
+
+
+def _divisor_near(W: int, target: int) -> int:
+    """Divisor of W closest to target (at least 1)."""
+    best = 1
+    for d in range(1, int(np.sqrt(W)) + 1):
+        if W % d == 0:
+            for q in (d, W // d):
+                if abs(q - target) < abs(best - target):
+                    best = q
+    return best
+
+
+def mixed_streams(n: int = 256, seed: int = 3, w_lo: int = 1_000, w_hi: int = 200_000) -> list:
+    """Uneven independent streams: dim 2 or 3 (50/50), W log-uniform in
+    [w_lo, w_hi], S a divisor of W near U[1%, 10%] of W, Gaussian-mixture data
+    (20 Gaussians, sigma 1, 10% uniform noise) in a box scaled so densities
+    differ per stream, Eps for a mean neighbour count drawn from U[10, 30]
+    (see mix_eps), MinPts U[4, 16]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        dim = 2 if rng.random() < 0.5 else 3
+        W = int(np.exp(rng.uniform(np.log(w_lo), np.log(w_hi))))
+        W = max(w_lo, (W // 100) * 100)
+        S = _divisor_near(W, int(W * rng.uniform(0.01, 0.10)))
+        box = float(rng.uniform(40.0, 160.0))
+        target = float(rng.uniform(10.0, 30.0))
+        eps = mix_eps(W, dim, box, target)
+        out.append(MixStream(dim, W, S, eps, int(rng.integers(4, 17)), 1000 + i, box))
+    return out
+
+
+def mix_eps(W: int, dim: int, box: float, target: float, k: int = 20, sigma: float = 1.0) -> float:
+    """Eps giving about `target` neighbours for a mixture point: cluster
+    points have density ~ n_c / (4 pi sigma^2)^(d/2) around them (a Gaussian
+    seen from its own samples), n_c = 0.9 W / k."""
+    n_c = 0.9 * W / k
+    dens = n_c / (4.0 * np.pi * sigma * sigma) ** (dim / 2.0)
+    vol = target / dens
+    if dim == 2:
+        return float(np.sqrt(vol / np.pi))
+    return float((vol * 3.0 / (4.0 * np.pi)) ** (1.0 / 3.0))
+
+
+def mix_points(s: MixStream, n_total: int) -> np.ndarray:
+    return gaussian_mixture(n_total, dim=s.dim, k=20, box=s.box, sigma=1.0, seed=s.seed)
