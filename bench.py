@@ -431,6 +431,9 @@ def run_batched(args, dev, stream, flush, n_streams=256, rounds=None, plain_roun
         _, elab, ecid, _ = oracle.window_grid(win, st.eps, st.min_pts, oracle.MODE_FP64)
         lab, cid = pool.outputs(ids[i])
         exact = exact and bool(np.array_equal(lab, elab) and np.array_equal(cid, ecid))
+    # one more round (the last round's points again) with every phase timed
+    prof = pool.slide_profiled(ids, packed[timed[-1]])
+    prof = {k: v for k, v in prof.items() if k.endswith("_ms")}
     stats = pool.stats()
     pool.close()
 
@@ -466,6 +469,7 @@ def run_batched(args, dev, stream, flush, n_streams=256, rounds=None, plain_roun
         "plain_one_at_a_time": {"value": plain_value, "round_ms": statistics.mean(plain_ms)},
         "speedup_vs_plain": value / plain_value,
         "launches_per_round": stats["launches_per_round"], "graph_replays": stats["graph_replays"],
+        "phase_ms": prof,
         "exact_sample_vs_fp64_oracle": exact,
     }
 

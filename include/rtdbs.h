@@ -254,6 +254,10 @@ RTDBS_API int rtdbs_pool_load_window(rtdbs_pool* pool, int32_t stream_id, const 
  * each stream's device buffers (rtdbs_pool_outputs). */
 RTDBS_API int rtdbs_pool_slide(rtdbs_pool* pool, int32_t n, const int32_t* stream_ids,
                                const float* d_points);
+/* rtdbs_pool_slide with every phase launched directly and bracketed by CUDA
+ * events (chunk phases summed); synchronous. */
+RTDBS_API int rtdbs_pool_slide_profiled(rtdbs_pool* pool, int32_t n, const int32_t* stream_ids,
+                                        const float* d_points, rtdbs_phase_times* times);
 /* Waits for the pool's stream; RTDBS_ERR_DEVICE if any stream hit a device bound. */
 RTDBS_API int rtdbs_pool_sync(rtdbs_pool* pool);
 RTDBS_API int rtdbs_pool_outputs(rtdbs_pool* pool, int32_t stream_id, int32_t** d_label,

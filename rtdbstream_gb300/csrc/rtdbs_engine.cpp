@@ -942,6 +942,72 @@ int rtdbs_pool_slide(rtdbs_pool* p, int32_t n, const int32_t* ids, const float* 
     return RTDBS_OK;
 }
 
+int rtdbs_pool_slide_profiled(rtdbs_pool* p, int32_t n, const int32_t* ids, const float* d_points,
+                              rtdbs_phase_times* t) {
+    if (!p || !t) return fail(RTDBS_ERR_INVALID, "pool/times is NULL");
+    if (n <= 0 || !ids || !d_points) return fail(RTDBS_ERR_INVALID, "ids/points is NULL or n <= 0");
+    std::vector<int> list(ids, ids + n);
+    std::vector<char> seen(p->capacity, 0);
+    for (int id : list) {
+        if (id < 0 || id >= p->capacity || !p->eng[id] || !p->loaded[id])
+            return fail(RTDBS_ERR_STATE, "stream %d is not loaded", id);
+        if (seen[id]) return fail(RTDBS_ERR_INVALID, "stream %d listed twice", id);
+        seen[id] = 1;
+    }
+    DeviceGuard guard(p->device);
+    CUDA_TRY(guard.err);
+    if (list != p->shape_ids) {
+        pool_drop_shape(p);
+        int rc = pool_build_shape(p, list);
+        if (rc != RTDBS_OK) return rc;
+    }
+    CUDA_TRY(cudaMemcpyAsync(p->d_input, d_points, sizeof(float) * p->input_floats, cudaMemcpyDeviceToDevice,
+                             p->stream));
+    std::vector<cudaEvent_t> ev(p->plan.size() + 1, nullptr);
+    for (auto& x : ev) CUDA_TRY(cudaEventCreate(&x));
+    int rc = RTDBS_OK;
+    cudaEventRecord(ev[0], p->stream);
+    for (size_t i = 0; i < p->plan.size() && rc == RTDBS_OK; ++i) {
+        const auto& l = p->plan[i];
+        rtdbs::BatchLaunch L;
+        L.views = p->d_views;
+        L.items = reinterpret_cast<const rtdbs::BatchItem*>(p->d_tables + l.items_off);
+        L.prefix = reinterpret_cast<const int*>(p->d_tables + l.prefix_off);
+        L.n = l.n;
+        cudaError_t ce = rtdbs::launch_batch(l.phase, L, l.blocks, l.max_c, p->stream);
+        if (ce != cudaSuccess) rc = fail(RTDBS_ERR_CUDA, "launch failed: %s", cudaGetErrorString(ce));
+        cudaEventRecord(ev[i + 1], p->stream);
+    }
+    if (rc == RTDBS_OK) rc = rtdbs_pool_sync(p);
+    if (rc == RTDBS_OK) {
+        // batch phases -> the engine's phase slots (sort + run merge are one)
+        static const int slot[rtdbs::kNumBatchPhases] = {0, 1, 1, 2, 3, 4, 5, 6, 7, 8};
+        float ph[9] = {0};
+        for (size_t i = 0; i < p->plan.size(); ++i) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+            ph[slot[p->plan[i].phase]] += ms;
+        }
+        float total = 0.f;
+        cudaEventElapsedTime(&total, ev[0], ev[p->plan.size()]);
+        t->ingest_ms = ph[0];
+        t->sort_ms = ph[1];
+        t->decrement_ms = ph[2];
+        t->merge_ms = ph[3];
+        t->build_ms = ph[4];
+        t->increment_ms = ph[5];
+        t->union_ms = ph[6];
+        t->flatten_ms = ph[7];
+        t->label_ms = ph[8];
+        t->total_ms = total;
+        t->chunks = 0;
+    }
+    for (auto& x : ev)
+        if (x) cudaEventDestroy(x);
+    ++p->rounds;
+    return rc;
+}
+
 int rtdbs_pool_sync(rtdbs_pool* p) {
     if (!p) return fail(RTDBS_ERR_INVALID, "pool is NULL");
     DeviceGuard guard(p->device);

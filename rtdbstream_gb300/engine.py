@@ -35,7 +35,7 @@ EXPORTED_SYMBOLS = (
     "rtdbs_stream_bytes", "rtdbs_pool_params_init", "rtdbs_pool_create", "rtdbs_pool_destroy",
     "rtdbs_pool_add_stream", "rtdbs_pool_remove_stream", "rtdbs_pool_load_window", "rtdbs_pool_slide",
     "rtdbs_pool_sync", "rtdbs_pool_outputs", "rtdbs_pool_read_outputs", "rtdbs_pool_engine",
-    "rtdbs_pool_get_stats",
+    "rtdbs_pool_get_stats", "rtdbs_pool_slide_profiled",
 )
 RTDBS_ERR_BUDGET = -7
 
@@ -127,6 +127,7 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     L.rtdbs_pool_read_outputs.argtypes = [vp, ctypes.c_int32, vp, vp, ctypes.c_int]
     L.rtdbs_pool_engine.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(vp)]
     L.rtdbs_pool_get_stats.argtypes = [vp, ctypes.POINTER(PoolStats)]
+    L.rtdbs_pool_slide_profiled.argtypes = [vp, ctypes.c_int32, vp, vp, ctypes.POINTER(PhaseTimes)]
     for name in EXPORTED_SYMBOLS:
         getattr(L, name).restype = getattr(L, name).restype or ctypes.c_int
     _lib = L
@@ -345,6 +346,12 @@ class Pool:
 
     def sync(self) -> None:
         _check(self._lib.rtdbs_pool_sync(self._h))
+
+    def slide_profiled(self, sids, d_points) -> dict:
+        ids = (ctypes.c_int32 * len(sids))(*[int(x) for x in sids])
+        t = PhaseTimes()
+        _check(self._lib.rtdbs_pool_slide_profiled(self._h, len(sids), ids, _ptr(d_points), ctypes.byref(t)))
+        return {f: getattr(t, f) for f, _ in PhaseTimes._fields_}
 
     def outputs(self, sid: int):
         W = self.windows[sid][0]
