@@ -971,6 +971,7 @@ __device__ __forceinline__ void label_body(const View& v, int advance, int bx, C
         const bool hv = lane < len;
         float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
         int hslot = -1, hr = -1;
+        bool lonely = false;
         if (hv) {
             h = spt[start + lane];
             hslot = slot_of(h);
@@ -978,9 +979,14 @@ __device__ __forceinline__ void label_body(const View& v, int advance, int bx, C
             if (hr >= 0) {
                 v.label[hslot] = 0;
                 v.cid[hslot] = hr;
+            } else if (v.scnt[cur][start + lane] <= 1) {
+                // no neighbour but itself: noise without a scan
+                lonely = true;
+                v.label[hslot] = 2;
+                v.cid[hslot] = hslot;
             }
         }
-        const unsigned nmask = __ballot_sync(kFull, hv && hr < 0);
+        const unsigned nmask = __ballot_sync(kFull, hv && hr < 0 && !lonely);
         if (!nmask) continue;
         __syncwarp();
         home_pt[wib][lane] = h;
@@ -1007,7 +1013,7 @@ __device__ __forceinline__ void label_body(const View& v, int advance, int bx, C
                 if (lane == hi) best = min(best, mn);
             }
         }
-        if (hv && hr < 0) {
+        if (hv && hr < 0 && !lonely) {
             if (best != INT_MAX) {
                 v.label[hslot] = 1;
                 v.cid[hslot] = best;
