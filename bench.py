@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-verify", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     # smaller windows of the same walker stream, for profiler captures only
     ap.add_argument("--window", type=int, default=None)
     ap.add_argument("--stride", type=int, default=None)
@@ -380,6 +381,8 @@ def run_ours(args) -> None:
     if not args.no_batched:
         del d_pts
         line["batched"] = run_batched(args, dev, stream, flush)
+    if not args.no_serving:
+        line["serving"] = run_serving(args, dev, stream)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -472,6 +475,42 @@ def run_batched(args, dev, stream, flush, n_streams=256, rounds=None, plain_roun
         "phase_ms": prof,
         "exact_sample_vs_fp64_oracle": exact,
     }
+
+
+def run_serving(args, dev, stream, n_streams=1000, loads=(0.3, 0.6, 0.9), duration=1.5, k_slides=4):
+    """Continuous-batching server over 1,000 streams (the batched mix),
+    Poisson slide requests at offered loads relative to the measured
+    all-stream round rate, HBM budget 120 GB; p50/p99 request latency
+    (arrival -> completion of its round) and slid points/s."""
+    import torch
+
+    from rtdbstream_gb300.serve import ServedStream, SlideServer, poisson_arrivals
+
+    specs = wl.mixed_streams(n_streams, seed=7)
+    srv = SlideServer(device=dev, hbm_budget_bytes=120 * 10**9, stream=stream.cuda_stream)
+    for sp in specs:
+        pts = wl.mix_points(sp, sp.window + k_slides * sp.stride)
+        data = torch.from_numpy(np.ascontiguousarray(pts[sp.window:]).reshape(k_slides, sp.stride * sp.dim)).to(dev)
+        srv.add(ServedStream(sp, pts[:sp.window], data))
+    # capacity: every stream in every round
+    t_all = np.zeros(3 * n_streams)
+    tgt_all = np.tile(np.arange(n_streams), 3)
+    cap = srv.run(t_all, tgt_all)
+    cap_rps = cap["requests"] / cap["wall_s"]
+    sweep = []
+    for f in loads:
+        rate = f * cap_rps
+        t, tgt = poisson_arrivals(rate, duration, n_streams, seed=int(f * 100))
+        r = srv.run(t, tgt)
+        sweep.append({"offered_requests_per_s": rate, "offered_fraction": f,
+                      **{k: r[k] for k in ("requests", "slid_points_per_s", "latency_ms_p50", "latency_ms_p99",
+                                           "mean_round_size")}})
+    st = srv.pool.stats()
+    srv.close()
+    return {"workload": f"{n_streams} streams (the batched mix, W 1k..200k), Poisson slide requests, "
+                        f"HBM budget 120 GB ({st['bytes_in_use'] / 1e9:.1f} GB admitted)",
+            "capacity_requests_per_s": cap_rps, "capacity_slid_points_per_s": cap["slid_points_per_s"],
+            "sweep": sweep}
 
 
 def main():

@@ -258,6 +258,11 @@ RTDBS_API int rtdbs_pool_slide(rtdbs_pool* pool, int32_t n, const int32_t* strea
  * events (chunk phases summed); synchronous. */
 RTDBS_API int rtdbs_pool_slide_profiled(rtdbs_pool* pool, int32_t n, const int32_t* stream_ids,
                                         const float* d_points, rtdbs_phase_times* times);
+/* The same round with each stream's new points in its own device buffer
+ * (d_points_each[i] holds S_i * dim_i floats of stream_ids[i]); one gather
+ * kernel packs them. */
+RTDBS_API int rtdbs_pool_slide_each(rtdbs_pool* pool, int32_t n, const int32_t* stream_ids,
+                                    const float* const* d_points_each);
 /* Waits for the pool's stream; RTDBS_ERR_DEVICE if any stream hit a device bound. */
 RTDBS_API int rtdbs_pool_sync(rtdbs_pool* pool);
 RTDBS_API int rtdbs_pool_outputs(rtdbs_pool* pool, int32_t stream_id, int32_t** d_label,

@@ -641,6 +641,8 @@ struct rtdbs_pool {
     size_t tables_cap = 0;
     float* d_input = nullptr;         // the round's new points, back to back
     size_t input_cap = 0;             // floats
+    void* d_gather = nullptr;         // per-stream source pointers, offsets, counts
+    size_t gather_cap = 0;
     std::vector<int> shape_ids;       // stream set the tables / graph were built for
     cudaGraphExec_t graph = nullptr;
     // launch plan of the cached shape
@@ -823,6 +825,7 @@ int rtdbs_pool_destroy(rtdbs_pool* p) {
     if (p->h_ctls) cudaFreeHost(p->h_ctls);
     if (p->d_tables) cudaFree(p->d_tables);
     if (p->d_input) cudaFree(p->d_input);
+    if (p->d_gather) cudaFree(p->d_gather);
     if (p->own_stream && p->stream) cudaStreamDestroy(p->stream);
     delete p;
     return RTDBS_OK;
@@ -897,8 +900,29 @@ int rtdbs_pool_load_window(rtdbs_pool* p, int32_t id, const float* points, int p
     return RTDBS_OK;
 }
 
+namespace {
+int pool_round(rtdbs_pool* p, int32_t n, const int32_t* ids, const float* d_points,
+               const float* const* d_points_each);
+}
+
 int rtdbs_pool_slide(rtdbs_pool* p, int32_t n, const int32_t* ids, const float* d_points) {
     if (!p || n <= 0 || !ids || !d_points) return fail(RTDBS_ERR_INVALID, "pool/ids/points is NULL or n <= 0");
+    return pool_round(p, n, ids, d_points, nullptr);
+}
+
+int rtdbs_pool_slide_each(rtdbs_pool* p, int32_t n, const int32_t* ids, const float* const* d_points_each) {
+    if (!p || n <= 0 || !ids || !d_points_each)
+        return fail(RTDBS_ERR_INVALID, "pool/ids/points is NULL or n <= 0");
+    for (int i = 0; i < n; ++i)
+        if (!d_points_each[i]) return fail(RTDBS_ERR_INVALID, "points of stream %d is NULL", ids[i]);
+    return pool_round(p, n, ids, nullptr, d_points_each);
+}
+
+}  // extern "C"
+
+namespace {
+int pool_round(rtdbs_pool* p, int32_t n, const int32_t* ids, const float* d_points,
+               const float* const* d_points_each) {
     std::vector<int> list(ids, ids + n);
     std::vector<char> seen(p->capacity, 0);
     for (int id : list) {
@@ -914,8 +938,38 @@ int rtdbs_pool_slide(rtdbs_pool* p, int32_t n, const int32_t* ids, const float* 
         int rc = pool_build_shape(p, list);
         if (rc != RTDBS_OK) return rc;
     }
-    CUDA_TRY(cudaMemcpyAsync(p->d_input, d_points, sizeof(float) * p->input_floats, cudaMemcpyDeviceToDevice,
-                             p->stream));
+    if (d_points) {
+        CUDA_TRY(cudaMemcpyAsync(p->d_input, d_points, sizeof(float) * p->input_floats,
+                                 cudaMemcpyDeviceToDevice, p->stream));
+    } else {
+        // one gather kernel packs the streams' own buffers
+        const size_t need = (size_t)n * (sizeof(void*) + sizeof(long long) + sizeof(int));
+        if (need > p->gather_cap) {
+            if (p->d_gather) cudaFree(p->d_gather);
+            p->d_gather = nullptr;
+            CUDA_TRY(cudaMalloc(&p->d_gather, need));
+            p->gather_cap = need;
+        }
+        std::vector<char> host(need);
+        const float** src = reinterpret_cast<const float**>(host.data());
+        long long* off = reinterpret_cast<long long*>(host.data() + (size_t)n * sizeof(void*));
+        int* cnt = reinterpret_cast<int*>(host.data() + (size_t)n * (sizeof(void*) + sizeof(long long)));
+        int max_count = 0;
+        for (int i = 0; i < n; ++i) {
+            const rtdbs_engine* e = p->eng[list[i]];
+            src[i] = d_points_each[i];
+            off[i] = (long long)p->input_off[i];
+            cnt[i] = e->p.stride * e->p.dim;
+            max_count = std::max(max_count, cnt[i]);
+        }
+        // pageable source: the call returns once the table is staged
+        CUDA_TRY(cudaMemcpyAsync(p->d_gather, host.data(), need, cudaMemcpyHostToDevice, p->stream));
+        char* g = static_cast<char*>(p->d_gather);
+        CUDA_TRY(rtdbs::launch_gather(reinterpret_cast<const float* const*>(g),
+                                      reinterpret_cast<const long long*>(g + (size_t)n * sizeof(void*)),
+                                      reinterpret_cast<const int*>(g + (size_t)n * (sizeof(void*) + sizeof(long long))),
+                                      p->d_input, n, max_count, p->stream));
+    }
     if (p->flags & RTDBS_FLAG_NO_GRAPH) {
         int rc = pool_enqueue_round(p);
         if (rc != RTDBS_OK) return rc;
@@ -941,6 +995,9 @@ int rtdbs_pool_slide(rtdbs_pool* p, int32_t n, const int32_t* ids, const float* 
     ++p->rounds;
     return RTDBS_OK;
 }
+}  // namespace
+
+extern "C" {
 
 int rtdbs_pool_slide_profiled(rtdbs_pool* p, int32_t n, const int32_t* ids, const float* d_points,
                               rtdbs_phase_times* t) {

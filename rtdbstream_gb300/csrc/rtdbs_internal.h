@@ -170,5 +170,9 @@ struct BatchLaunch {
 int batch_blocks(int phase, const View& v, int c);
 int batch_threads(int phase);
 cudaError_t launch_batch(int phase, const BatchLaunch& L, int total_blocks, int max_c, cudaStream_t s);
+// Packs n device arrays (count[i] floats from src[i]) into dst at dst_off[i];
+// the three tables are device memory.
+cudaError_t launch_gather(const float* const* src, const long long* dst_off, const int* count, float* dst,
+                          int n, int max_count, cudaStream_t s);
 
 }  // namespace rtdbs

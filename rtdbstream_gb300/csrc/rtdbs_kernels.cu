@@ -1292,6 +1292,24 @@ cudaError_t launch_batch(int phase, const BatchLaunch& L, int total_blocks, int 
     return cudaGetLastError();
 }
 
+// Copies n separate point arrays into one packed buffer: block (x, y) moves
+// part of array y.
+__global__ void k_gather(const float* const* src, const long long* dst_off, const int* count, float* dst) {
+    const int y = blockIdx.y;
+    const float* a = src[y];
+    float* d = dst + dst_off[y];
+    const int n = count[y];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) d[i] = a[i];
+}
+
+cudaError_t launch_gather(const float* const* src, const long long* dst_off, const int* count, float* dst,
+                          int n, int max_count, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int bx = max(1, min(64, (max_count + 1023) / 1024));
+    k_gather<<<dim3(bx, n), 1024, 0, s>>>(src, dst_off, count, dst);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_counts_by_slot(const View& v, int* nn, cudaStream_t s) {
     const int sms = g_num_sms > 0 ? g_num_sms : 152;
     k_counts_by_slot<<<sms * 4, 256, 0, s>>>(v, nn);

@@ -35,7 +35,7 @@ EXPORTED_SYMBOLS = (
     "rtdbs_stream_bytes", "rtdbs_pool_params_init", "rtdbs_pool_create", "rtdbs_pool_destroy",
     "rtdbs_pool_add_stream", "rtdbs_pool_remove_stream", "rtdbs_pool_load_window", "rtdbs_pool_slide",
     "rtdbs_pool_sync", "rtdbs_pool_outputs", "rtdbs_pool_read_outputs", "rtdbs_pool_engine",
-    "rtdbs_pool_get_stats", "rtdbs_pool_slide_profiled",
+    "rtdbs_pool_get_stats", "rtdbs_pool_slide_profiled", "rtdbs_pool_slide_each",
 )
 RTDBS_ERR_BUDGET = -7
 
@@ -128,6 +128,7 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     L.rtdbs_pool_engine.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(vp)]
     L.rtdbs_pool_get_stats.argtypes = [vp, ctypes.POINTER(PoolStats)]
     L.rtdbs_pool_slide_profiled.argtypes = [vp, ctypes.c_int32, vp, vp, ctypes.POINTER(PhaseTimes)]
+    L.rtdbs_pool_slide_each.argtypes = [vp, ctypes.c_int32, vp, vp]
     for name in EXPORTED_SYMBOLS:
         getattr(L, name).restype = getattr(L, name).restype or ctypes.c_int
     _lib = L
@@ -343,6 +344,14 @@ class Pool:
         their new points back to back in that order."""
         ids = (ctypes.c_int32 * len(sids))(*[int(x) for x in sids])
         _check(self._lib.rtdbs_pool_slide(self._h, len(sids), ids, _ptr(d_points)))
+
+    def slide_each(self, sids, d_points_each) -> None:
+        """One round with each stream's new points in its own device buffer
+        (a sequence of tensors or raw device addresses)."""
+        n = len(sids)
+        ids = (ctypes.c_int32 * n)(*[int(x) for x in sids])
+        ptrs = (ctypes.c_void_p * n)(*[x if isinstance(x, int) else _ptr(x) for x in d_points_each])
+        _check(self._lib.rtdbs_pool_slide_each(self._h, n, ids, ptrs))
 
     def sync(self) -> None:
         _check(self._lib.rtdbs_pool_sync(self._h))
