@@ -69,6 +69,22 @@ def parse():
     return args
 
 
+def weak_scaling_value(local_ms: float, steps: int, stride: int, world: int, device: str = "cpu"):
+    """Whole-job slid points/s of `world` independent streams, one per rank:
+    every rank slid steps * stride points; the job time is the slowest rank's
+    (MAX over ranks).  Returns (value, max_ms)."""
+    total_ms = local_ms
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([local_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+        total_ms = float(t.item())
+    return world * steps * stride / (total_ms / 1000.0), total_ms
+
+
 def walker_stream(n_total: int, seed: int) -> np.ndarray:
     """The walker stream; a smaller window keeps 500 points per walker trail
     (2,000 walkers at W = 1M), so the local density matches the full size."""
@@ -294,13 +310,7 @@ def run_ours(args) -> None:
         eng.sync()
         torch.cuda.synchronize()
     per_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = float(sum(per_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.barrier()
-        total_ms = float(t.item())
-    value = world * args.steps * S / (total_ms / 1000.0)
+    value, total_ms = weak_scaling_value(float(sum(per_ms)), args.steps, S, world, f"cuda:{dev}")
 
     # end to end through the host-buffer API (pinned buffers)
     h_pts = torch.from_numpy(pts).pin_memory().numpy()
@@ -378,10 +388,10 @@ def run_ours(args) -> None:
         "exact_vs_fp64_oracle": verified,
         "band_rechecks": st["band_rechecks"],
     }
-    if not args.no_batched:
+    if not args.no_batched and world == 1:
         del d_pts
         line["batched"] = run_batched(args, dev, stream, flush)
-    if not args.no_serving:
+    if not args.no_serving and world == 1:
         line["serving"] = run_serving(args, dev, stream)
     print(json.dumps(line), flush=True)
     if world > 1:
