@@ -207,6 +207,23 @@ RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int32_t n, int
 RTDBS_API int rtdbs_slide_profiled(rtdbs_engine* engine, const float* d_new_points,
                                    rtdbs_phase_times* times);
 
+/* ------------------------------------------------------------- data files
+ * Readers for the reference's dataset formats (src/dbscan/util.cpp:12-254):
+ * the format comes from the file name like the reference's
+ * (src/dbscan/dbscan.cpp:2454-2470) or is given explicitly. */
+#define RTDBS_FORMAT_AUTO    0
+#define RTDBS_FORMAT_TAO     1  /* text "x,y,z" per line (3-D) */
+#define RTDBS_FORMAT_GEOLIFE 2  /* binary double triples (3-D) */
+#define RTDBS_FORMAT_RBF     3  /* header line, then "x,y" (2-D) */
+#define RTDBS_FORMAT_EDS     4  /* header line, then "id x y cid" (2-D) */
+#define RTDBS_FORMAT_STOCK   5  /* header line, then one value (1-D) */
+
+/* Reads up to n_max points into xyz[n_max][3] (missing coordinates 0);
+ * *n_read points were read, *dim is the format's dimension, and bbox_min /
+ * bbox_max (3 floats each, may be NULL) bound the finite coordinates read. */
+RTDBS_API int rtdbs_read_points(const char* path, int32_t format, int64_t n_max, float* xyz,
+                                int64_t* n_read, int32_t* dim, float* bbox_min, float* bbox_max);
+
 /* ------------------------------------------------------------------ pools
  * A pool slides many independent streams together: one launch per kernel
  * phase covers every stream of a round (each with its own W, S, dim, Eps,

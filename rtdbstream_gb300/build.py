@@ -2,9 +2,11 @@
 
     python -m rtdbstream_gb300.build
 
-Sources: csrc/rtdbs_kernels.cu (device code) and csrc/rtdbs_engine.cpp (the
-C ABI of include/rtdbs.h).  Both translation units compile in parallel; the
-result lands in rtdbstream_gb300/_build/ (git-ignored).
+Sources: csrc/rtdbs_kernels.cu (device code), csrc/rtdbs_engine.cpp (the C
+ABI of include/rtdbs.h: engines and pools), csrc/rtdbs_noalloc.cu and
+csrc/rtdbs_io.cpp; the translation units compile in parallel.  Also builds
+rtdbs_dbscan, the reference-compatible command line (csrc/rtdbs_cli.cpp).
+Results land in rtdbstream_gb300/_build/ (git-ignored).
 """
 from __future__ import annotations
 
@@ -18,6 +20,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "librtdbs.so")
+CLI = os.path.join(OUT_DIR, "rtdbs_dbscan")  # the reference-compatible command line
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -30,7 +33,7 @@ def nvcc() -> str:
 
 def sources() -> list[str]:
     return [os.path.join(CSRC, "rtdbs_kernels.cu"), os.path.join(CSRC, "rtdbs_engine.cpp"),
-            os.path.join(CSRC, "rtdbs_noalloc.cu")]
+            os.path.join(CSRC, "rtdbs_noalloc.cu"), os.path.join(CSRC, "rtdbs_io.cpp")]
 
 
 def headers() -> list[str]:
@@ -41,7 +44,8 @@ def up_to_date() -> bool:
     if not os.path.exists(LIB):
         return False
     t = os.path.getmtime(LIB)
-    return all(os.path.getmtime(f) <= t for f in sources() + headers() + [__file__])
+    srcs = sources() + headers() + [__file__, os.path.join(CSRC, "rtdbs_cli.cpp")]
+    return os.path.exists(CLI) and all(os.path.getmtime(f) <= t for f in srcs)
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
@@ -72,6 +76,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}{r.stderr}")
     os.replace(tmp, LIB)
+    cli = [nvcc(), *ARCH, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+           os.path.join(CSRC, "rtdbs_cli.cpp"), "-o", CLI + ".tmp", "-L", OUT_DIR, "-lrtdbs",
+           "-Xlinker", "-rpath,$ORIGIN"]
+    r = subprocess.run(cli, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"CLI build failed:\n{r.stdout}{r.stderr}")
+    os.replace(CLI + ".tmp", CLI)
     return LIB
 
 

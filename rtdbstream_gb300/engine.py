@@ -35,7 +35,7 @@ EXPORTED_SYMBOLS = (
     "rtdbs_stream_bytes", "rtdbs_pool_params_init", "rtdbs_pool_create", "rtdbs_pool_destroy",
     "rtdbs_pool_add_stream", "rtdbs_pool_remove_stream", "rtdbs_pool_load_window", "rtdbs_pool_slide",
     "rtdbs_pool_sync", "rtdbs_pool_outputs", "rtdbs_pool_read_outputs", "rtdbs_pool_engine",
-    "rtdbs_pool_get_stats", "rtdbs_pool_slide_profiled", "rtdbs_pool_slide_each",
+    "rtdbs_pool_get_stats", "rtdbs_pool_slide_profiled", "rtdbs_pool_slide_each", "rtdbs_read_points",
 )
 RTDBS_ERR_BUDGET = -7
 
@@ -129,6 +129,8 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     L.rtdbs_pool_get_stats.argtypes = [vp, ctypes.POINTER(PoolStats)]
     L.rtdbs_pool_slide_profiled.argtypes = [vp, ctypes.c_int32, vp, vp, ctypes.POINTER(PhaseTimes)]
     L.rtdbs_pool_slide_each.argtypes = [vp, ctypes.c_int32, vp, vp]
+    L.rtdbs_read_points.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.c_int64, vp,
+                                    ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32), vp, vp]
     for name in EXPORTED_SYMBOLS:
         getattr(L, name).restype = getattr(L, name).restype or ctypes.c_int
     _lib = L
@@ -380,3 +382,21 @@ class Pool:
         s = PoolStats()
         _check(self._lib.rtdbs_pool_get_stats(self._h, ctypes.byref(s)))
         return {f: getattr(s, f) for f, _ in PoolStats._fields_ if not f.startswith("reserved")}
+
+
+FORMATS = {"auto": 0, "tao": 1, "geolife": 2, "rbf": 3, "eds": 4, "stock": 5}
+
+
+def read_points(path: str, n_max: int, fmt: str = "auto"):
+    """Reads a point file in one of the reference's formats.  Returns
+    (points [n, dim] float32, bbox_min [dim], bbox_max [dim])."""
+    xyz = np.zeros((max(int(n_max), 0), 3), np.float32)
+    n = ctypes.c_int64()
+    dim = ctypes.c_int32()
+    lo = np.zeros(3, np.float32)
+    hi = np.zeros(3, np.float32)
+    _check(load_library().rtdbs_read_points(os.fsencode(path), FORMATS[fmt.lower()], int(n_max),
+                                            xyz.ctypes.data, ctypes.byref(n), ctypes.byref(dim),
+                                            lo.ctypes.data, hi.ctypes.data))
+    d = dim.value
+    return np.ascontiguousarray(xyz[: n.value, :d]), lo[:d].copy(), hi[:d].copy()
