@@ -387,6 +387,7 @@ def run_ours(args) -> None:
         "clocks": clk.summary(),
         "exact_vs_fp64_oracle": verified,
         "band_rechecks": st["band_rechecks"],
+        "dist_tests_per_slide": st["dist_tests"] / max(1, st["slides"]),
     }
     if not args.no_batched and world == 1:
         del d_pts

@@ -101,7 +101,9 @@ typedef struct rtdbs_stats {
     int64_t device_bytes;    /* device memory owned by the engine */
     int32_t launches_per_slide; /* kernels launched by one slide */
     int32_t chunks_per_slide;   /* grid-update chunks per slide (ceil(S / 16384)) */
-    int64_t reserved[3];
+    int64_t dist_tests;         /* distance tests evaluated, cumulative (the reference's
+                                   DEBUG_INFO num_dist_calculations, src/dbscan/dbscan.cpp:145-212) */
+    int64_t reserved[2];
 } rtdbs_stats;
 
 /* Per-phase device time of one profiled slide, in milliseconds (the

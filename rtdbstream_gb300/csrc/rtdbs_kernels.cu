@@ -117,16 +117,22 @@ __device__ __forceinline__ double sqdist64(const float4& a, const float4& b) {
 // d32 < r2f.  FP64 mode: d32 < lo and d32 >= hi are decided by the float
 // value (the band [lo, hi) around Eps^2 bounds the float evaluation's
 // rounding error, see oracle_band); everything else in double.
+// Per-thread counters: distance tests, and those re-decided in FP64.
+struct Tally {
+    unsigned tests = 0;
+    unsigned rechecks = 0;
+};
+
 template <int MODE, int DIM>
-__device__ __forceinline__ bool is_nbr(const View& v, const float4& a, const float4& b,
-                                       unsigned& rechecks) {
+__device__ __forceinline__ bool is_nbr(const View& v, const float4& a, const float4& b, Tally& t) {
+    ++t.tests;
     const float d = sqdist32<DIM>(a, b);
     if (MODE == kPrecFp32) return d < v.r2f;
     if (v.filter_ok) {
         if (d < v.lo) return true;
         if (d >= v.hi) return false;
     }
-    ++rechecks;
+    ++t.rechecks;
     return sqdist64<DIM>(a, b) < v.E;
 }
 
@@ -299,13 +305,13 @@ __device__ __forceinline__ int uf_link(int* parent, int a, int b, int& err) {
     return a < b ? a : b;
 }
 
-__device__ __forceinline__ void flush_stats(const View& v, unsigned rechecks, int err, int lane) {
-    unsigned r = rechecks;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(kFull, r, o);
+__device__ __forceinline__ void flush_stats(const View& v, const Tally& t, int err, int lane) {
+    const unsigned r = __reduce_add_sync(kFull, t.rechecks);
+    const unsigned n = __reduce_add_sync(kFull, t.tests);
     const int e = __reduce_or_sync(kFull, (unsigned)err);
     if (lane == 0) {
         if (r) atomicAdd(&v.ctl->band_rechecks, (unsigned long long)r);
+        if (n) atomicAdd(&v.ctl->dist_tests, (unsigned long long)n);
         if (e) atomicOr(&v.ctl->err, e);
     }
 }
@@ -496,15 +502,15 @@ __device__ __forceinline__ void decr_body(const View& v, int j, int c, int bx, S
     const int total = candidate_stream<DIM>(rs, re, 0, lane, rstart[wib], rpre[wib]);
     const float4* spt = v.spt[old];
     int* scnt = v.scnt[old];
-    unsigned rechecks = 0;
+    Tally tally;
     int r = 0;
     for (int idx = lane; idx < total; idx += 32) {
         const int pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
         const float4 q = spt[pos];
         const int qs = slot_of(q);
-        if ((qs < el || qs >= el + c) && is_nbr<MODE, DIM>(v, xp, q, rechecks)) atomicSub(&scnt[pos], 1);
+        if ((qs < el || qs >= el + c) && is_nbr<MODE, DIM>(v, xp, q, tally)) atomicSub(&scnt[pos], 1);
     }
-    flush_stats(v, rechecks, 0, lane);
+    flush_stats(v, tally, 0, lane);
 }
 
 template <int MODE, int DIM>
@@ -776,7 +782,7 @@ __device__ __forceinline__ void incr_body(const View& v, int j, int c, int init,
     const int total = candidate_stream<DIM>(rs, re, 0, lane, rstart[wib], rpre[wib]);
     const float4* spt = v.spt[cur];
     int* scnt = v.scnt[cur];
-    unsigned rechecks = 0;
+    Tally tally;
     int count = 0, mypos = -1, r = 0;
     for (int idx = lane; idx < total; idx += 32) {
         const int pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
@@ -785,7 +791,7 @@ __device__ __forceinline__ void incr_body(const View& v, int j, int c, int init,
         if (qs == aslot) {
             ++count;
             mypos = pos;
-        } else if (is_nbr<MODE, DIM>(v, ap, q, rechecks)) {
+        } else if (is_nbr<MODE, DIM>(v, ap, q, tally)) {
             ++count;
             if (qs < el || qs >= el + c) atomicAdd(&scnt[pos], 1);
         }
@@ -800,7 +806,7 @@ __device__ __forceinline__ void incr_body(const View& v, int j, int c, int init,
         else
             err = kErrChunk;
     }
-    flush_stats(v, rechecks, err, lane);
+    flush_stats(v, tally, err, lane);
 }
 
 template <int MODE, int DIM>
@@ -844,7 +850,7 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
     // each to the point's own slot): coalesced with the candidate loads, and
     // refreshed as roots are found, so find walks stay short.
     volatile int* hint = v.sroot;
-    unsigned rechecks = 0;
+    Tally tally;
     int err = 0;
     // Warps take batches of kBatch consecutive work items (neighbouring
     // cells: candidate loads reuse L1) from a counter, so uneven items do not
@@ -897,7 +903,7 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
             while (mm) {
                 const int hi = __ffs(mm) - 1;
                 mm &= mm - 1;
-                if (qc && pos > start + hi && qh != rh[hi] && is_nbr<MODE, DIM>(v, hpt[hi], q, rechecks))
+                if (qc && pos > start + hi && qh != rh[hi] && is_nbr<MODE, DIM>(v, hpt[hi], q, tally))
                     adj |= 1u << hi;
             }
             if (adj) {
@@ -917,7 +923,7 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
         }
         if (hcore) hint[start + lane] = rh[lane];
     }
-    flush_stats(v, rechecks, err, lane);
+    flush_stats(v, tally, err, lane);
 }
 
 template <int MODE, int DIM>
@@ -956,7 +962,7 @@ __device__ __forceinline__ void label_body(const View& v, int advance, int bx, C
     const int* sroot = v.sroot;
     const unsigned long long* skey = v.skey[cur];
     const ulonglong2* T = v.table[cur];
-    unsigned rechecks = 0;
+    Tally tally;
     int it1 = 0;
     for (int itx = nitems;;) {
         if (itx >= it1) {
@@ -1008,7 +1014,7 @@ __device__ __forceinline__ void label_body(const View& v, int advance, int bx, C
             while (mm) {
                 const int hi = __ffs(mm) - 1;
                 mm &= mm - 1;
-                const int val = (qr >= 0 && is_nbr<MODE, DIM>(v, hpt[hi], q, rechecks)) ? qr : INT_MAX;
+                const int val = (qr >= 0 && is_nbr<MODE, DIM>(v, hpt[hi], q, tally)) ? qr : INT_MAX;
                 const int mn = (int)__reduce_min_sync(kFull, (unsigned)val);
                 if (lane == hi) best = min(best, mn);
             }
@@ -1023,7 +1029,7 @@ __device__ __forceinline__ void label_body(const View& v, int advance, int bx, C
             }
         }
     }
-    flush_stats(v, rechecks, 0, lane);
+    flush_stats(v, tally, 0, lane);
     if (bx == 0 && threadIdx.x == 0) {
         v.ctl->union_next = 0;                // the next clustering's queue; not read here
         if (advance) v.ctl->slide += 1;       // no reader here

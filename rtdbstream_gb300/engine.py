@@ -54,7 +54,7 @@ class Stats(ctypes.Structure):
                 ("error_bits", ctypes.c_int32), ("key_bits", ctypes.c_int32),
                 ("cell_side", ctypes.c_double), ("device_bytes", ctypes.c_int64),
                 ("launches_per_slide", ctypes.c_int32), ("chunks_per_slide", ctypes.c_int32),
-                ("reserved", ctypes.c_int64 * 3)]
+                ("dist_tests", ctypes.c_int64), ("reserved", ctypes.c_int64 * 2)]
 
 
 PHASES = ("ingest", "sort", "decrement", "merge", "build", "increment", "union", "flatten", "label")

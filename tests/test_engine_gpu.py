@@ -108,6 +108,7 @@ def test_streams_match_oracle(name, gen, W, S, eps, mp, slides, precision):
     mode = O.MODE_FP64 if precision == "fp64" else O.MODE_FP32
     exp = O.stream(pts, W, S, eps, mp, mode, first_slide=1, n_out=slides)
     assert_same(got[:3], exp, f"{name}/{precision}")
+    assert got[3]["dist_tests"] > 0 and got[3]["slides"] == slides
     if name.startswith("band") and precision == "fp64":
         assert got[3]["band_rechecks"] > 0
         # the FP64 relation really differs from the reference's FP32 one here
