@@ -530,7 +530,7 @@ int rtdbs_get_stats(rtdbs_engine* e, rtdbs_stats* s) {
     std::memset(s, 0, sizeof(*s));
     s->slides = e->h_ctl->slide;
     s->band_rechecks = (int64_t)e->h_ctl->band_rechecks;
-    s->dist_tests = (int64_t)e->h_ctl->dist_tests;
+    for (int k = 0; k < 8; ++k) s->dist_tests += (int64_t)e->h_ctl->dist_tests[k];
     s->cells = e->h_ctl->ncells;
     s->work_items = e->h_ctl->nitems;
     s->error_bits = e->h_ctl->err;

@@ -58,7 +58,7 @@ struct Ctl {
     int union_next;            // next work item handed out by k_union
     int label_next;            // next work item handed out by k_label
     unsigned long long band_rechecks;
-    unsigned long long dist_tests;   // distance tests evaluated
+    unsigned long long dist_tests[8];  // distance tests evaluated, spread over 8 counters
     long long reserved[3];
 };
 

@@ -311,7 +311,7 @@ __device__ __forceinline__ void flush_stats(const View& v, const Tally& t, int e
     const int e = __reduce_or_sync(kFull, (unsigned)err);
     if (lane == 0) {
         if (r) atomicAdd(&v.ctl->band_rechecks, (unsigned long long)r);
-        if (n) atomicAdd(&v.ctl->dist_tests, (unsigned long long)n);
+        if (n) atomicAdd(&v.ctl->dist_tests[(threadIdx.x >> 5) & 7], (unsigned long long)n);
         if (e) atomicOr(&v.ctl->err, e);
     }
 }
