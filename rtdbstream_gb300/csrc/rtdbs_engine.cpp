@@ -186,6 +186,13 @@ size_t plan_layout(rtdbs_engine* e, std::vector<Part>& parts) {
     v.pbits = pbits;
     v.pmask = (unsigned)(P - 1);
     v.max_items = W + W / 32 + 64;
+    // Neighbour lists of non-core points (MinPts - 2 entries each) replace the
+    // label pass's grid scan up to kListCap entries; above that the scan stays.
+    const int mp = e->p.min_pts;
+    v.list_cap = (mp >= 2 && mp - 2 <= rtdbs::kListCap) ? mp - 2 : -1;
+    const size_t list_ints = v.list_cap > 0 ? (size_t)W * v.list_cap : 0;
+    const size_t track_ints = v.list_cap >= 0 ? (size_t)W : 0;
+    v.nlist = v.ntrack = v.relist = nullptr;
     parts = {
         {(void**)&v.ring, sizeof(float4) * W},
         {(void**)&v.kslot, sizeof(unsigned long long) * W},
@@ -202,6 +209,9 @@ size_t plan_layout(rtdbs_engine* e, std::vector<Part>& parts) {
         {(void**)&v.sroot, sizeof(int) * W},
         {(void**)&v.label, sizeof(int) * W},
         {(void**)&v.cid, sizeof(int) * W},
+        {(void**)&v.nlist, sizeof(int) * list_ints},
+        {(void**)&v.ntrack, sizeof(int) * track_ints},
+        {(void**)&v.relist, sizeof(int) * 2 * track_ints},
         {(void**)&v.nsort, sizeof(unsigned long long) * C},
         {(void**)&v.xsort, sizeof(unsigned long long) * C},
         {(void**)&v.nword, sizeof(unsigned long long) * C},
@@ -238,7 +248,7 @@ int allocate(rtdbs_engine* e) {
 int check_device_error(rtdbs_engine* e) {
     if (e->h_ctl->err)
         return fail(RTDBS_ERR_DEVICE, "device error bits 0x%x (1 table full, 2 union-find bound, "
-                    "4 work list full, 8 chunk bookkeeping)", e->h_ctl->err);
+                    "4 work list full, 8 chunk bookkeeping, 16 neighbour lists)", e->h_ctl->err);
     return RTDBS_OK;
 }
 
@@ -539,7 +549,8 @@ int rtdbs_get_stats(rtdbs_engine* e, rtdbs_stats* s) {
     s->device_bytes = (int64_t)e->dev_bytes;
     const int nchunks = (e->p.stride + e->chunk - 1) / e->chunk;
     s->chunks_per_slide = nchunks;
-    s->launches_per_slide = nchunks * (rtdbs::kChunkPhases + 1) + 3;  // sort phase = 2 kernels
+    // sort phase = 2 kernels; label phase = relist + border with neighbour lists
+    s->launches_per_slide = nchunks * (rtdbs::kChunkPhases + 1) + (e->v.list_cap >= 0 ? 4 : 3);
     return RTDBS_OK;
 }
 
@@ -1039,7 +1050,8 @@ int rtdbs_pool_slide_profiled(rtdbs_pool* p, int32_t n, const int32_t* ids, cons
     if (rc == RTDBS_OK) rc = rtdbs_pool_sync(p);
     if (rc == RTDBS_OK) {
         // batch phases -> the engine's phase slots (sort + run merge are one)
-        static const int slot[rtdbs::kNumBatchPhases] = {0, 1, 1, 2, 3, 4, 5, 6, 7, 8};
+        // (the list rebuild belongs to the label phase, as in the single-stream launch)
+        static const int slot[rtdbs::kNumBatchPhases] = {0, 1, 1, 2, 3, 4, 5, 6, 7, 8, 8};
         float ph[9] = {0};
         for (size_t i = 0; i < p->plan.size(); ++i) {
             float ms = 0.f;

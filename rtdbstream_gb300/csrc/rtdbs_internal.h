@@ -17,6 +17,11 @@
 //   sroot  i32[W]         per sorted position: root hint during the union, then
 //                         the root (-1: not core)
 //   label, cid i32[W]     outputs by slot
+//   nlist  i32[W][cap]    neighbour list of every non-core point by slot
+//                         (cap = MinPts - 2 entries; -1 = empty entry)
+//   ntrack i32[W]         1: the slot's list is exact; 0: not kept (core);
+//                         2: not kept, queued for a rebuild
+//   relist i32[2W]        slots queued for a list rebuild this slide
 //   chunk scratch: sort words, expired points.
 #pragma once
 
@@ -37,12 +42,14 @@ constexpr int kBuildThreads = 512;
 constexpr int kClusterThreads = 256;
 constexpr int kBatch = 8;          // work items a clustering warp takes at a time
 constexpr int kMaxIter = 1 << 20;  // bound on every device-side retry loop
+constexpr int kListCap = 30;       // longest neighbour list kept (MinPts <= 32)
 
 // Bits of Ctl::err.
 constexpr int kErrHashFull = 1;
 constexpr int kErrUnionIter = 2;
 constexpr int kErrItems = 4;
 constexpr int kErrChunk = 8;
+constexpr int kErrList = 16;
 
 // Device-resident control block of one stream.  Every field that changes
 // from slide to slide lives here (not in kernel arguments), so one captured
@@ -54,7 +61,7 @@ struct Ctl {
     int nitems;                // work items of the current grid
     int ncells;                // cells of the current grid
     int err;                   // kErr* bits
-    int pad0;
+    int relist_n;              // slots queued in View::relist this slide
     int union_next;            // next work item handed out by k_union
     int label_next;            // next work item handed out by k_label
     unsigned long long band_rechecks;
@@ -84,6 +91,8 @@ struct View {
     int sort_passes;
     int max_items;
     int precision;              // RTDBS_PREC_* (batched launches dispatch on it)
+    int list_cap;               // entries per neighbour list; -1: no lists (the
+                                // label pass then scans the grid)
     // buffers
     float4* ring;
     unsigned long long* kslot;
@@ -97,6 +106,9 @@ struct View {
                                  // then the root (-1: not core)
     int* label;
     int* cid;
+    int* nlist;                  // [W][list_cap] neighbours of non-core points
+    int* ntrack;                 // per slot: list state (1 exact, 0 not kept, 2 queued)
+    int* relist;                 // [2W] slots whose lists are rebuilt this slide
     unsigned long long* nsort;   // chunk sort words in (key << 14 | offset)
     unsigned long long* xsort;
     unsigned long long* nword;   // sorted
@@ -147,6 +159,7 @@ enum BatchPhase : int {
     kBatchIncrement,
     kBatchUnion,
     kBatchFlatten,
+    kBatchRelist,
     kBatchLabel,
     kNumBatchPhases
 };

@@ -286,20 +286,24 @@ __device__ __forceinline__ int uf_find(int* parent, int v) {
     return curr;
 }
 
-// Lock-free union of the sets of a and b (any ancestors of the two points):
-// the larger root is hooked under the smaller with atomicCAS, so every root
-// is the minimum slot of its set.  Returns an ancestor of both afterwards.
-__device__ __forceinline__ int uf_link(int* parent, int a, int b, int& err) {
+// Lock-free union of the sets of a and b, each an ancestor of one of the two
+// points (a cached or freshly found root; it need not still be a root).  The
+// larger of the two is hooked under the smaller with one atomicCAS, which only
+// succeeds on a root; on failure the walk resumes from the root that the CAS
+// revealed.  max(a, b) falls every round, so the loop ends, and parents only
+// ever point to smaller slots, so every root is the minimum slot of its set.
+// Returns an ancestor of both points afterwards.
+__device__ __forceinline__ int uf_hook(int* parent, int a, int b, int& err) {
     for (int it = 0; it < kMaxIter; ++it) {
-        a = uf_find(parent, a);
-        b = uf_find(parent, b);
         if (a == b) return a;
         if (a < b) {
             const int t = a;
             a = b;
             b = t;
         }
-        if (atomicCAS(&parent[a], a, b) == a) return b;
+        const int old = atomicCAS(&parent[a], a, b);
+        if (old == a) return b;
+        a = uf_find(parent, old);
     }
     err |= kErrUnionIter;
     return a < b ? a : b;
@@ -314,6 +318,65 @@ __device__ __forceinline__ void flush_stats(const View& v, const Tally& t, int e
         if (n) atomicAdd(&v.ctl->dist_tests[(threadIdx.x >> 5) & 7], (unsigned long long)n);
         if (e) atomicOr(&v.ctl->err, e);
     }
+}
+
+// ------------------------------------------------------- neighbour lists
+// Every non-core point keeps the slots of its neighbours (at most MinPts - 2
+// besides itself) in a fixed list by slot, maintained from the same distance
+// tests that keep the counts exact: an expired neighbour is removed in the
+// decrement pass, a new one appended in the increment pass.  A point that
+// becomes core stops keeping its list (ntrack 0); one that drops back below
+// MinPts is queued and its list rebuilt by one scan once the slide's counts
+// are final.  The label pass then reads lists instead of scanning the grid.
+
+// Appends slot p to q's list (q tracked); a full list means q has reached
+// MinPts, so it stops being kept.
+__device__ __forceinline__ void list_append(const View& v, int q, int p) {
+    int* L = v.nlist + (size_t)q * v.list_cap;
+    for (int k = 0; k < v.list_cap; ++k)
+        if (L[k] == -1 && atomicCAS(&L[k], -1, p) == -1) return;
+    v.ntrack[q] = 0;
+}
+
+// Removes slot p from q's list (q tracked; only this thread removes p).
+__device__ __forceinline__ void list_remove(const View& v, int q, int p) {
+    int* L = v.nlist + (size_t)q * v.list_cap;
+    for (int k = 0; k < v.list_cap; ++k)
+        if (L[k] == p) {
+            L[k] = -1;
+            return;
+        }
+    atomicOr(&v.ctl->err, kErrList);
+}
+
+// Queues slot q (just fell below MinPts, list not kept) for a rebuild, once.
+__device__ __forceinline__ void relist_push(const View& v, int q) {
+    if (atomicCAS(&v.ntrack[q], 0, 2) != 0) return;
+    const int at = atomicAdd(&v.ctl->relist_n, 1);
+    if (at < 2 * v.W)
+        v.relist[at] = q;
+    else
+        atomicOr(&v.ctl->err, kErrList);
+}
+
+// Warp-wide: adds the lanes' neighbour slots (nb) to the warp's buffer in
+// lane order; returns the new number found (entries past cap are dropped,
+// the list is then not kept anyway).
+__device__ __forceinline__ int list_collect(bool nb, int qs, int nfound, int cap, int* buf, int lane) {
+    const unsigned m = __ballot_sync(kFull, nb);
+    const int at = nfound + __popc(m & lanemask_lt(lane));
+    if (nb && at < cap) buf[at] = qs;
+    return nfound + __popc(m);
+}
+
+// Warp-wide: writes slot a's list from the buffer (kept iff a is not core).
+__device__ __forceinline__ void list_store(const View& v, int a, int nfound, const int* buf, int lane) {
+    __syncwarp();
+    const bool keep = nfound + 1 < v.min_pts;
+    int* L = v.nlist + (size_t)a * v.list_cap;
+    for (int k = lane; k < v.list_cap; k += 32) L[k] = (keep && k < nfound) ? buf[k] : -1;
+    if (lane == 0) v.ntrack[a] = keep ? 1 : 0;
+    __syncwarp();
 }
 
 // ------------------------------------------------------------------- kernels
@@ -481,6 +544,7 @@ __global__ void __launch_bounds__(kSortRun) k_runmerge(View v, int c, int init) 
 // -1 on the count of every surviving neighbour of each expired point (old grid).
 struct StreamSmem {
     int rstart[8][9], rpre[8][10];
+    int nbuf[8][kListCap];
 };
 
 template <int MODE, int DIM>
@@ -502,13 +566,23 @@ __device__ __forceinline__ void decr_body(const View& v, int j, int c, int bx, S
     const int total = candidate_stream<DIM>(rs, re, 0, lane, rstart[wib], rpre[wib]);
     const float4* spt = v.spt[old];
     int* scnt = v.scnt[old];
+    const bool lists = v.list_cap >= 0;
+    const int xs = slot_of(xp);
     Tally tally;
     int r = 0;
     for (int idx = lane; idx < total; idx += 32) {
         const int pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
         const float4 q = spt[pos];
         const int qs = slot_of(q);
-        if ((qs < el || qs >= el + c) && is_nbr<MODE, DIM>(v, xp, q, tally)) atomicSub(&scnt[pos], 1);
+        if ((qs < el || qs >= el + c) && is_nbr<MODE, DIM>(v, xp, q, tally)) {
+            const int was = atomicSub(&scnt[pos], 1);
+            if (lists) {
+                if (was == v.min_pts)
+                    relist_push(v, qs);
+                else if (was < v.min_pts && v.ntrack[qs] == 1)
+                    list_remove(v, qs, xs);
+            }
+        }
     }
     flush_stats(v, tally, 0, lane);
 }
@@ -782,20 +856,33 @@ __device__ __forceinline__ void incr_body(const View& v, int j, int c, int init,
     const int total = candidate_stream<DIM>(rs, re, 0, lane, rstart[wib], rpre[wib]);
     const float4* spt = v.spt[cur];
     int* scnt = v.scnt[cur];
+    const bool lists = v.list_cap >= 0;
+    int* nbuf = sm.nbuf[wib];
     Tally tally;
-    int count = 0, mypos = -1, r = 0;
-    for (int idx = lane; idx < total; idx += 32) {
-        const int pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
-        const float4 q = spt[pos];
-        const int qs = slot_of(q);
-        if (qs == aslot) {
-            ++count;
-            mypos = pos;
-        } else if (is_nbr<MODE, DIM>(v, ap, q, tally)) {
-            ++count;
-            if (qs < el || qs >= el + c) atomicAdd(&scnt[pos], 1);
+    int count = 0, mypos = -1, r = 0, nfound = 0;
+    for (int base = 0; base < total; base += 32) {
+        const int idx = base + lane;
+        bool nb = false;
+        int qs = -1;
+        if (idx < total) {
+            const int pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
+            const float4 q = spt[pos];
+            qs = slot_of(q);
+            if (qs == aslot) {
+                ++count;
+                mypos = pos;
+            } else if (is_nbr<MODE, DIM>(v, ap, q, tally)) {
+                ++count;
+                nb = true;
+                if (qs < el || qs >= el + c) {
+                    atomicAdd(&scnt[pos], 1);
+                    if (lists && v.ntrack[qs] == 1) list_append(v, qs, aslot);
+                }
+            }
         }
+        if (lists) nfound = list_collect(nb, qs, nfound, v.list_cap, nbuf, lane);
     }
+    if (lists) list_store(v, aslot, nfound, nbuf, lane);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) count += __shfl_xor_sync(kFull, count, o);
     mypos = (int)__reduce_max_sync(kFull, (unsigned)(mypos + 1)) - 1;
@@ -890,11 +977,10 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
             bool qc = false;
             if (idx < total) {
                 pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
-                qc = scnt[pos] >= v.min_pts;
-                if (qc) {
-                    q = spt[pos];
-                    qh = hint[pos];
-                }
+                const int qn = scnt[pos];
+                q = spt[pos];
+                qh = hint[pos];
+                qc = qn >= v.min_pts;
             }
             if (!__any_sync(kFull, qc)) continue;
             // Pairs whose hints already agree are in one set: no test, no link.
@@ -913,7 +999,7 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
                     adj &= adj - 1;
                     const int ra = rh[hi];
                     if (ra != rq) {
-                        rq = uf_link(parent, ra, rq, err);
+                        rq = uf_hook(parent, ra, rq, err);
                         rh[hi] = rq;  // an ancestor of both points (benign race)
                     }
                 }
@@ -927,18 +1013,31 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
 }
 
 template <int MODE, int DIM>
-__global__ void __launch_bounds__(kClusterThreads, 6) k_union(View v) {
+__global__ void __launch_bounds__(kClusterThreads, 8) k_union(View v) {
     __shared__ ClusterSmem sm;
     union_body<MODE, DIM>(v, sm);
 }
 
-// Root of every core point by sorted position (-1 for non-core points),
-// walked from the position's root hint.
+// Root of every core point, walked from the position's root hint.  Without
+// neighbour lists: by sorted position (-1 for non-core points), for the grid
+// scan of k_label.  With lists: straight to the outputs by slot, core -> 0
+// and its root, non-core -> 2 and its own slot (k_border then turns the
+// non-core points next to a core into border points).
 __device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx) {
     if (bx == 0 && threadIdx.x == 0) v.ctl->label_next = 0;  // k_label's queue; not read here
     const int cur = (int)(v.ctl->b & 1);
     const int n = v.ctl->nocc[cur];
     const int* scnt = v.scnt[cur];
+    if (v.list_cap >= 0) {
+        const int* sw = reinterpret_cast<const int*>(v.spt[cur]) + 3;  // .w = slot
+        for (int i = bx * blockDim.x + threadIdx.x; i < n; i += nbx * blockDim.x) {
+            const int slot = sw[4 * (size_t)i];
+            const bool core = scnt[i] >= v.min_pts;
+            v.label[slot] = core ? 0 : 2;
+            v.cid[slot] = core ? uf_find(v.parent, v.sroot[i]) : slot;
+        }
+        return;
+    }
     for (int i = bx * blockDim.x + threadIdx.x; i < n; i += nbx * blockDim.x)
         v.sroot[i] = scnt[i] >= v.min_pts ? uf_find(v.parent, v.sroot[i]) : -1;
 }
@@ -1007,7 +1106,7 @@ __device__ __forceinline__ void label_body(const View& v, int advance, int bx, C
             if (idx < total) {
                 const int pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
                 qr = sroot[pos];
-                if (qr >= 0) q = spt[pos];
+                q = spt[pos];
             }
             if (!__any_sync(kFull, qr >= 0)) continue;
             unsigned mm = nmask;
@@ -1042,6 +1141,79 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advanc
     label_body<MODE, DIM>(v, advance, blockIdx.x, sm);
 }
 
+// Rebuilds the lists of the queued slots (points that fell below MinPts this
+// slide) from one scan of the final grid; warp per queued slot.
+template <int MODE, int DIM>
+__device__ __forceinline__ void relist_body(const View& v, int bx, int nbx, StreamSmem& sm) {
+    int(&rstart)[8][9] = sm.rstart;
+    int(&rpre)[8][10] = sm.rpre;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const long long b = v.ctl->b;
+    const int cur = (int)(b & 1);
+    const unsigned gen = gen_of_build(b);
+    const int n = min(v.ctl->relist_n, 2 * v.W);
+    const float4* spt = v.spt[cur];
+    int* nbuf = sm.nbuf[wib];
+    Tally tally;
+    for (int e = bx * wpb + wib; e < n; e += nbx * wpb) {
+        const int a = v.relist[e];
+        const float4 ap = v.ring[a];
+        int rs, re;
+        row_ranges<DIM>(v, v.table[cur], gen, v.kslot[a], lane, rs, re);
+        const int total = candidate_stream<DIM>(rs, re, 0, lane, rstart[wib], rpre[wib]);
+        int r = 0, nfound = 0;
+        for (int base = 0; base < total; base += 32) {
+            const int idx = base + lane;
+            bool nb = false;
+            int qs = -1;
+            if (idx < total) {
+                const float4 q = spt[stream_pos(idx, r, rstart[wib], rpre[wib])];
+                qs = slot_of(q);
+                nb = qs != a && is_nbr<MODE, DIM>(v, ap, q, tally);
+            }
+            nfound = list_collect(nb, qs, nfound, v.list_cap, nbuf, lane);
+        }
+        list_store(v, a, nfound, nbuf, lane);
+    }
+    flush_stats(v, tally, 0, lane);
+}
+
+template <int MODE, int DIM>
+__global__ void __launch_bounds__(256) k_relist(View v) {
+    __shared__ StreamSmem sm;
+    relist_body<MODE, DIM>(v, blockIdx.x, gridDim.x, sm);
+}
+
+// Border points from the lists: a non-core point (label 2 after the flatten)
+// with a core neighbour gets label 1 and the minimum root over its core
+// neighbours.  Ends the slide like k_label.
+__device__ __forceinline__ void border_body(const View& v, int advance, int bx, int nbx) {
+    for (int s = bx * blockDim.x + threadIdx.x; s < v.W; s += nbx * blockDim.x) {
+        if (v.label[s] == 0) continue;
+        if (v.ntrack[s] != 1) {
+            atomicOr(&v.ctl->err, kErrList);
+            continue;
+        }
+        const int* L = v.nlist + (size_t)s * v.list_cap;
+        int best = INT_MAX;
+        for (int k = 0; k < v.list_cap; ++k) {
+            const int q = L[k];
+            if (q >= 0 && v.label[q] == 0) best = min(best, v.cid[q]);
+        }
+        if (best != INT_MAX) {
+            v.label[s] = 1;
+            v.cid[s] = best;
+        }
+    }
+    if (bx == 0 && threadIdx.x == 0) {
+        v.ctl->union_next = 0;                // the next clustering's queue; not read here
+        v.ctl->relist_n = 0;                  // rebuilds done
+        if (advance) v.ctl->slide += 1;       // no reader here
+    }
+}
+
+__global__ void k_border(View v, int advance) { border_body(v, advance, blockIdx.x, gridDim.x); }
+
 __global__ void k_counts_by_slot(View v, int* nn) {
     const int cur = (int)(v.ctl->b & 1);
     const int n = v.ctl->nocc[cur];
@@ -1074,8 +1246,9 @@ template <> struct PhaseShape<kBatchDecrement> { static constexpr int threads = 
 template <> struct PhaseShape<kBatchMerge> { static constexpr int threads = kMergeThreads, min_blocks = 1; };
 template <> struct PhaseShape<kBatchBuild> { static constexpr int threads = kBuildThreads, min_blocks = 1; };
 template <> struct PhaseShape<kBatchIncrement> { static constexpr int threads = 256, min_blocks = 1; };
-template <> struct PhaseShape<kBatchUnion> { static constexpr int threads = kClusterThreads, min_blocks = 6; };
+template <> struct PhaseShape<kBatchUnion> { static constexpr int threads = kClusterThreads, min_blocks = 8; };
 template <> struct PhaseShape<kBatchFlatten> { static constexpr int threads = 256, min_blocks = 1; };
+template <> struct PhaseShape<kBatchRelist> { static constexpr int threads = 256, min_blocks = 1; };
 template <> struct PhaseShape<kBatchLabel> { static constexpr int threads = kClusterThreads, min_blocks = 6; };
 
 // One phase over many streams.  The block finds its item, copies that
@@ -1135,9 +1308,15 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
         RTDBS_BODY_DISPATCH(prec, dim, union_body, sv, sm);
     } else if constexpr (PHASE == kBatchFlatten) {
         flatten_body(sv, bx, nbx);
+    } else if constexpr (PHASE == kBatchRelist) {
+        __shared__ StreamSmem sm;
+        if (sv.list_cap >= 0) RTDBS_BODY_DISPATCH(prec, dim, relist_body, sv, bx, nbx, sm);
     } else {
         __shared__ ClusterSmem sm;
-        RTDBS_BODY_DISPATCH(prec, dim, label_body, sv, 1, bx, sm);
+        if (sv.list_cap >= 0)
+            border_body(sv, 1, bx, nbx);
+        else
+            RTDBS_BODY_DISPATCH(prec, dim, label_body, sv, 1, bx, sm);
     }
 }
 
@@ -1207,14 +1386,21 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
         case kPhaseIncrement:
             RTDBS_DISPATCH(precision, v.dim, k_incr, warp_blocks, 256, s, v, j, c, init);
             break;
-        case kPhaseUnion:
-        case kPhaseLabel: {
+        case kPhaseLabel:
+            if (v.list_cap >= 0) {
+                const int sms = g_num_sms > 0 ? g_num_sms : 152;
+                RTDBS_DISPATCH(precision, v.dim, k_relist, sms, 256, s, v);
+                k_border<<<max(1, min(sms * 8, (v.W + 255) / 256)), 256, 0, s>>>(v, advance);
+                break;
+            }
+            [[fallthrough]];
+        case kPhaseUnion: {
             const int sms = g_num_sms > 0 ? g_num_sms : 152;
             const int per_block = kClusterThreads / 32;
             const int need = (v.max_items + per_block - 1) / per_block;  // one warp per item at most
             const int blocks = max(1, min(sms * 6, need));
             if (phase == kPhaseUnion)
-                RTDBS_DISPATCH(precision, v.dim, k_union, blocks, kClusterThreads, s, v);
+                RTDBS_DISPATCH(precision, v.dim, k_union, max(1, min(sms * 8, need)), kClusterThreads, s, v);
             else
                 RTDBS_DISPATCH(precision, v.dim, k_label, blocks, kClusterThreads, s, v, advance);
             break;
@@ -1270,8 +1456,11 @@ int batch_blocks(int phase, const View& v, int c) {
         case kBatchMerge: return (v.W + kMergeTile - 1) / kMergeTile;
         case kBatchBuild: return (v.W + kBuildThreads - 1) / kBuildThreads;
         case kBatchUnion:
-        case kBatchLabel: return max(1, min(1024, (v.W + 4095) / 4096));  // persistent, queue-fed
+        case kBatchLabel:
+            if (v.list_cap >= 0) return max(1, min(1024, (v.W + 1023) / 1024));  // k_border
+            return max(1, min(1024, (v.W + 4095) / 4096));  // persistent, queue-fed
         case kBatchFlatten: return max(1, min(1024, (v.W + 2047) / 2048));
+        case kBatchRelist: return v.list_cap >= 0 ? max(1, min(64, (v.W + 16383) / 16384)) : 0;
         default: return 0;
     }
 }
@@ -1292,6 +1481,7 @@ cudaError_t launch_batch(int phase, const BatchLaunch& L, int total_blocks, int 
         case kBatchIncrement: k_batch<kBatchIncrement><<<total_blocks, t, 0, s>>>(L); break;
         case kBatchUnion: k_batch<kBatchUnion><<<total_blocks, t, 0, s>>>(L); break;
         case kBatchFlatten: k_batch<kBatchFlatten><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchRelist: k_batch<kBatchRelist><<<total_blocks, t, 0, s>>>(L); break;
         case kBatchLabel: k_batch<kBatchLabel><<<total_blocks, t, 0, s>>>(L); break;
         default: return cudaErrorInvalidValue;
     }

@@ -97,6 +97,12 @@ CASES = [
     ("big_stride_W40k_S20k", lambda: wl.gaussian_mixture(40_000 + 3 * 20_000, dim=2, k=30, box=100.0, seed=7),
      40_000, 20_000, 0.4, 6, 3),
     ("S_eq_W_3d", lambda: wl.gaussian_mixture(3_000 * 4, dim=3, k=6, box=15.0, seed=8), 3_000, 3_000, 1.0, 5, 3),
+    # MinPts 32: the longest neighbour lists kept (30 entries)
+    ("mix3d_mp32_W12k", lambda: wl.gaussian_mixture(12_000 + 4 * 1_200, dim=3, k=10, box=30.0, seed=11),
+     12_000, 1_200, 0.9, 32, 4),
+    # MinPts 40: no lists, the label pass scans the grid
+    ("mix2d_mp40_W8k", lambda: wl.gaussian_mixture(8_000 + 4 * 800, dim=2, k=8, box=30.0, seed=12),
+     8_000, 800, 0.6, 40, 4),
 ]
 
 
