@@ -17,8 +17,10 @@
 //   sroot  i32[W]         per sorted position: root hint during the union, then
 //                         the root (-1: not core)
 //   label, cid i32[W]     outputs by slot
-//   nlist  i32[W][cap]    neighbour list of every non-core point by slot
-//                         (cap = MinPts - 2 entries; -1 = empty entry)
+//   nlist  i32[W][stride] neighbour list of every non-core point by slot
+//                         (cap = MinPts - 2 entries, rows padded to a multiple
+//                         of 4 for 16-byte loads; -1 = empty entry)
+//   rslot  i32[W]         per slot after the flatten: root (core) or -1
 //   ntrack i32[W]         1: the slot's list is exact; 0: not kept (core);
 //                         2: not kept, queued for a rebuild
 //   relist i32[2W]        slots queued for a list rebuild this slide
@@ -93,6 +95,7 @@ struct View {
     int precision;              // RTDBS_PREC_* (batched launches dispatch on it)
     int list_cap;               // entries per neighbour list; -1: no lists (the
                                 // label pass then scans the grid)
+    int list_stride;            // ints per list row (list_cap rounded up to 4)
     // buffers
     float4* ring;
     unsigned long long* kslot;
@@ -106,7 +109,8 @@ struct View {
                                  // then the root (-1: not core)
     int* label;
     int* cid;
-    int* nlist;                  // [W][list_cap] neighbours of non-core points
+    int* nlist;                  // [W][list_stride] neighbours of non-core points
+    int* rslot;                  // per slot: root of a core, -1 otherwise
     int* ntrack;                 // per slot: list state (1 exact, 0 not kept, 2 queued)
     int* relist;                 // [2W] slots whose lists are rebuilt this slide
     unsigned long long* nsort;   // chunk sort words in (key << 14 | offset)

@@ -187,29 +187,42 @@ __device__ bool table_set(ulonglong2* T, unsigned pmask, int pbits, unsigned lon
     return false;
 }
 
-// Row ranges of the 3^DIM cells around `key`.  The three cells of a row
-// (last axis -1, 0, +1) have consecutive keys, so they occupy one contiguous
-// range of the cell-sorted window.  On return lane r < 3^(DIM-1) holds row r
-// as [rs, re) (empty rows: rs == re).
-template <int DIM>
+// Rows of the 3^DIM stencil: the cells (last axis -1, 0, +1) of one row have
+// consecutive keys, so a row is one contiguous range of the cell-sorted
+// window.  The full stencil has 3^(DIM-1) rows.  The upper half (HALF) keeps
+// only the rows whose keys are not below the home cell's -- the centre row
+// (without its -1 cell) and the rows after it in key order -- since every
+// position below the home cell is clipped away by a pair-once union anyway.
+template <int DIM, bool HALF>
+struct Stencil {
+    static constexpr int kAllRows = DIM == 1 ? 1 : (DIM == 2 ? 3 : 9);
+    static constexpr int kFirst = HALF ? (kAllRows - 1) / 2 : 0;  // first row kept
+    static constexpr int kRows = kAllRows - kFirst;
+};
+
+// Row ranges of the stencil around `key`.  On return lane r < kRows holds
+// row r as [rs, re) (empty rows: rs == re).
+template <int DIM, bool HALF>
 __device__ __forceinline__ void row_ranges(const View& v, const ulonglong2* T, unsigned gen,
                                            unsigned long long key, int lane, int& rs, int& re) {
-    constexpr int kCells = DIM == 1 ? 3 : (DIM == 2 ? 9 : 27);
+    using St = Stencil<DIM, HALF>;
     const long long c2 = (long long)(key & ((1ull << v.shift[1]) - 1ull));
     const long long c1 = (long long)((key >> v.shift[1]) & ((1ull << (v.shift[0] - v.shift[1])) - 1ull));
     const long long c0 = (long long)(key >> v.shift[0]);
     int2 rg = make_int2(0, 0);
-    if (lane < kCells) {
+    const int row = St::kFirst + lane / 3, d_last = lane % 3 - 1;  // lane = 3 * kept row + cell
+    const bool skip = HALF && lane < 3 && d_last < 0;             // centre row, cell -1
+    if (lane < 3 * St::kRows && !skip) {
         long long q0 = c0, q1 = c1, q2 = c2;
         if (DIM == 1) {
-            q0 += lane - 1;
+            q0 += d_last;
         } else if (DIM == 2) {
-            q0 += lane / 3 - 1;
-            q1 += lane % 3 - 1;
+            q0 += row - 1;
+            q1 += d_last;
         } else {
-            q0 += lane / 9 - 1;
-            q1 += (lane / 3) % 3 - 1;
-            q2 += lane % 3 - 1;
+            q0 += row / 3 - 1;
+            q1 += row % 3 - 1;
+            q2 += d_last;
         }
         const bool ok = q0 >= 0 && q0 < v.ext[0] && q1 >= 0 && q1 < v.ext[1] && q2 >= 0 && q2 < v.ext[2];
         if (ok) {
@@ -234,29 +247,28 @@ __device__ __forceinline__ void row_ranges(const View& v, const ulonglong2* T, u
     re = e;
 }
 
-// The warp's row ranges (lanes 0..kRows-1), clipped below at `lo`, laid end
+// The warp's row ranges (lanes 0..ROWS-1), clipped below at `lo`, laid end
 // to end: candidate idx in [0, total) lives at sorted position
 // start[r] + idx - pre[r] for the row r with pre[r] <= idx < pre[r+1].
 // Concatenating the rows keeps the 32-lane candidate chunks full.
-template <int DIM>
+template <int ROWS>
 __device__ __forceinline__ int candidate_stream(int rs, int re, int lo, int lane, int* sstart,
                                                 int* spre) {
-    constexpr int kRows = DIM == 1 ? 1 : (DIM == 2 ? 3 : 9);
     const int a = max(rs, lo);
-    const int len = lane < kRows ? max(re - a, 0) : 0;
+    const int len = lane < ROWS ? max(re - a, 0) : 0;
     int incl = len;
 #pragma unroll
     for (int o = 1; o < 16; o <<= 1) {
         const int t = __shfl_up_sync(kFull, incl, o);
         if (lane >= o) incl += t;
     }
-    const int total = __shfl_sync(kFull, incl, kRows - 1);
+    const int total = __shfl_sync(kFull, incl, ROWS - 1);
     __syncwarp();
-    if (lane < kRows) {
+    if (lane < ROWS) {
         sstart[lane] = a;
         spre[lane] = incl - len;
     }
-    if (lane == 0) spre[kRows] = total;
+    if (lane == 0) spre[ROWS] = total;
     __syncwarp();
     return total;
 }
@@ -332,7 +344,7 @@ __device__ __forceinline__ void flush_stats(const View& v, const Tally& t, int e
 // Appends slot p to q's list (q tracked); a full list means q has reached
 // MinPts, so it stops being kept.
 __device__ __forceinline__ void list_append(const View& v, int q, int p) {
-    int* L = v.nlist + (size_t)q * v.list_cap;
+    int* L = v.nlist + (size_t)q * v.list_stride;
     for (int k = 0; k < v.list_cap; ++k)
         if (L[k] == -1 && atomicCAS(&L[k], -1, p) == -1) return;
     v.ntrack[q] = 0;
@@ -340,7 +352,7 @@ __device__ __forceinline__ void list_append(const View& v, int q, int p) {
 
 // Removes slot p from q's list (q tracked; only this thread removes p).
 __device__ __forceinline__ void list_remove(const View& v, int q, int p) {
-    int* L = v.nlist + (size_t)q * v.list_cap;
+    int* L = v.nlist + (size_t)q * v.list_stride;
     for (int k = 0; k < v.list_cap; ++k)
         if (L[k] == p) {
             L[k] = -1;
@@ -369,12 +381,13 @@ __device__ __forceinline__ int list_collect(bool nb, int qs, int nfound, int cap
     return nfound + __popc(m);
 }
 
-// Warp-wide: writes slot a's list from the buffer (kept iff a is not core).
+// Warp-wide: writes slot a's list from the buffer (kept iff a is not core);
+// the row's padding past list_cap stays -1.
 __device__ __forceinline__ void list_store(const View& v, int a, int nfound, const int* buf, int lane) {
     __syncwarp();
     const bool keep = nfound + 1 < v.min_pts;
-    int* L = v.nlist + (size_t)a * v.list_cap;
-    for (int k = lane; k < v.list_cap; k += 32) L[k] = (keep && k < nfound) ? buf[k] : -1;
+    int* L = v.nlist + (size_t)a * v.list_stride;
+    for (int k = lane; k < v.list_stride; k += 32) L[k] = (keep && k < nfound) ? buf[k] : -1;
     if (lane == 0) v.ntrack[a] = keep ? 1 : 0;
     __syncwarp();
 }
@@ -562,8 +575,8 @@ __device__ __forceinline__ void decr_body(const View& v, int j, int c, int bx, S
     const unsigned long long key = word >> kOffBits;
     const float4 xp = v.xpt[word & ((1u << kOffBits) - 1)];
     int rs, re;
-    row_ranges<DIM>(v, v.table[old], gen, key, lane, rs, re);
-    const int total = candidate_stream<DIM>(rs, re, 0, lane, rstart[wib], rpre[wib]);
+    row_ranges<DIM, false>(v, v.table[old], gen, key, lane, rs, re);
+    const int total = candidate_stream<Stencil<DIM, false>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
     const float4* spt = v.spt[old];
     int* scnt = v.scnt[old];
     const bool lists = v.list_cap >= 0;
@@ -852,8 +865,8 @@ __device__ __forceinline__ void incr_body(const View& v, int j, int c, int init,
     const int aslot = el + (int)(word & ((1u << kOffBits) - 1));
     const float4 ap = v.ring[aslot];
     int rs, re;
-    row_ranges<DIM>(v, v.table[cur], gen, key, lane, rs, re);
-    const int total = candidate_stream<DIM>(rs, re, 0, lane, rstart[wib], rpre[wib]);
+    row_ranges<DIM, false>(v, v.table[cur], gen, key, lane, rs, re);
+    const int total = candidate_stream<Stencil<DIM, false>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
     const float4* spt = v.spt[cur];
     int* scnt = v.scnt[cur];
     const bool lists = v.list_cap >= 0;
@@ -967,8 +980,8 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
         home_pt[wib][lane] = h;
         const int hmin = start + __ffs(hmask) - 1;
         int rs, re;
-        row_ranges<DIM>(v, T, gen, skey[start], lane, rs, re);
-        const int total = candidate_stream<DIM>(rs, re, hmin + 1, lane, rstart[wib], rpre[wib]);
+        row_ranges<DIM, true>(v, T, gen, skey[start], lane, rs, re);
+        const int total = candidate_stream<Stencil<DIM, true>::kRows>(rs, re, hmin + 1, lane, rstart[wib], rpre[wib]);
         int r = 0;
         for (int base = 0; base < total; base += 32) {
             const int idx = base + lane;
@@ -1020,9 +1033,8 @@ __global__ void __launch_bounds__(kClusterThreads, 8) k_union(View v) {
 
 // Root of every core point, walked from the position's root hint.  Without
 // neighbour lists: by sorted position (-1 for non-core points), for the grid
-// scan of k_label.  With lists: straight to the outputs by slot, core -> 0
-// and its root, non-core -> 2 and its own slot (k_border then turns the
-// non-core points next to a core into border points).
+// scan of k_label.  With lists: by slot (rslot), which k_border turns into
+// the outputs.
 __device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx) {
     if (bx == 0 && threadIdx.x == 0) v.ctl->label_next = 0;  // k_label's queue; not read here
     const int cur = (int)(v.ctl->b & 1);
@@ -1030,12 +1042,8 @@ __device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx) {
     const int* scnt = v.scnt[cur];
     if (v.list_cap >= 0) {
         const int* sw = reinterpret_cast<const int*>(v.spt[cur]) + 3;  // .w = slot
-        for (int i = bx * blockDim.x + threadIdx.x; i < n; i += nbx * blockDim.x) {
-            const int slot = sw[4 * (size_t)i];
-            const bool core = scnt[i] >= v.min_pts;
-            v.label[slot] = core ? 0 : 2;
-            v.cid[slot] = core ? uf_find(v.parent, v.sroot[i]) : slot;
-        }
+        for (int i = bx * blockDim.x + threadIdx.x; i < n; i += nbx * blockDim.x)
+            v.rslot[sw[4 * (size_t)i]] = scnt[i] >= v.min_pts ? uf_find(v.parent, v.sroot[i]) : -1;
         return;
     }
     for (int i = bx * blockDim.x + threadIdx.x; i < n; i += nbx * blockDim.x)
@@ -1096,8 +1104,8 @@ __device__ __forceinline__ void label_body(const View& v, int advance, int bx, C
         __syncwarp();
         home_pt[wib][lane] = h;
         int rs, re;
-        row_ranges<DIM>(v, T, gen, skey[start], lane, rs, re);
-        const int total = candidate_stream<DIM>(rs, re, 0, lane, rstart[wib], rpre[wib]);
+        row_ranges<DIM, false>(v, T, gen, skey[start], lane, rs, re);
+        const int total = candidate_stream<Stencil<DIM, false>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
         int best = INT_MAX, r = 0;
         for (int base = 0; base < total; base += 32) {
             const int idx = base + lane;
@@ -1159,8 +1167,8 @@ __device__ __forceinline__ void relist_body(const View& v, int bx, int nbx, Stre
         const int a = v.relist[e];
         const float4 ap = v.ring[a];
         int rs, re;
-        row_ranges<DIM>(v, v.table[cur], gen, v.kslot[a], lane, rs, re);
-        const int total = candidate_stream<DIM>(rs, re, 0, lane, rstart[wib], rpre[wib]);
+        row_ranges<DIM, false>(v, v.table[cur], gen, v.kslot[a], lane, rs, re);
+        const int total = candidate_stream<Stencil<DIM, false>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
         int r = 0, nfound = 0;
         for (int base = 0; base < total; base += 32) {
             const int idx = base + lane;
@@ -1184,26 +1192,34 @@ __global__ void __launch_bounds__(256) k_relist(View v) {
     relist_body<MODE, DIM>(v, blockIdx.x, gridDim.x, sm);
 }
 
-// Border points from the lists: a non-core point (label 2 after the flatten)
-// with a core neighbour gets label 1 and the minimum root over its core
-// neighbours.  Ends the slide like k_label.
+// Outputs by slot from the roots and the lists: core -> 0 and its root; a
+// non-core point with a core neighbour -> 1 and the minimum root over its
+// core neighbours; else noise -> 2 and its own slot.  Ends the slide like
+// k_label.
 __device__ __forceinline__ void border_body(const View& v, int advance, int bx, int nbx) {
     for (int s = bx * blockDim.x + threadIdx.x; s < v.W; s += nbx * blockDim.x) {
-        if (v.label[s] == 0) continue;
-        if (v.ntrack[s] != 1) {
-            atomicOr(&v.ctl->err, kErrList);
-            continue;
+        const int root = v.rslot[s];
+        int lab = 0, id = root;
+        if (root < 0) {
+            if (v.ntrack[s] != 1) atomicOr(&v.ctl->err, kErrList);
+            const int4* L = reinterpret_cast<const int4*>(v.nlist + (size_t)s * v.list_stride);
+            int best = INT_MAX;
+            for (int k = 0; k < (v.list_stride >> 2); ++k) {
+                const int4 e = L[k];
+                const int r0 = e.x >= 0 ? v.rslot[e.x] : -1;
+                const int r1 = e.y >= 0 ? v.rslot[e.y] : -1;
+                const int r2 = e.z >= 0 ? v.rslot[e.z] : -1;
+                const int r3 = e.w >= 0 ? v.rslot[e.w] : -1;
+                if (r0 >= 0) best = min(best, r0);
+                if (r1 >= 0) best = min(best, r1);
+                if (r2 >= 0) best = min(best, r2);
+                if (r3 >= 0) best = min(best, r3);
+            }
+            lab = best != INT_MAX ? 1 : 2;
+            id = best != INT_MAX ? best : s;
         }
-        const int* L = v.nlist + (size_t)s * v.list_cap;
-        int best = INT_MAX;
-        for (int k = 0; k < v.list_cap; ++k) {
-            const int q = L[k];
-            if (q >= 0 && v.label[q] == 0) best = min(best, v.cid[q]);
-        }
-        if (best != INT_MAX) {
-            v.label[s] = 1;
-            v.cid[s] = best;
-        }
+        v.label[s] = lab;
+        v.cid[s] = id;
     }
     if (bx == 0 && threadIdx.x == 0) {
         v.ctl->union_next = 0;                // the next clustering's queue; not read here
