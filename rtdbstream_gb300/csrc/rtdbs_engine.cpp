@@ -193,7 +193,7 @@ size_t plan_layout(rtdbs_engine* e, std::vector<Part>& parts) {
     v.list_stride = v.list_cap > 0 ? (v.list_cap + 3) / 4 * 4 : 0;
     const size_t list_ints = (size_t)W * v.list_stride;
     const size_t track_ints = v.list_cap >= 0 ? (size_t)W : 0;
-    v.nlist = v.ntrack = v.relist = v.rslot = nullptr;
+    v.nlist = v.ntrack = v.rslot = nullptr;
     parts = {
         {(void**)&v.ring, sizeof(float4) * W},
         {(void**)&v.kslot, sizeof(unsigned long long) * W},
@@ -213,7 +213,6 @@ size_t plan_layout(rtdbs_engine* e, std::vector<Part>& parts) {
         {(void**)&v.nlist, sizeof(int) * list_ints},
         {(void**)&v.ntrack, sizeof(int) * track_ints},
         {(void**)&v.rslot, sizeof(int) * track_ints},
-        {(void**)&v.relist, sizeof(int) * 2 * track_ints},
         {(void**)&v.nsort, sizeof(unsigned long long) * C},
         {(void**)&v.xsort, sizeof(unsigned long long) * C},
         {(void**)&v.nword, sizeof(unsigned long long) * C},

@@ -21,9 +21,8 @@
 //                         (cap = MinPts - 2 entries, rows padded to a multiple
 //                         of 4 for 16-byte loads; -1 = empty entry)
 //   rslot  i32[W]         per slot after the flatten: root (core) or -1
-//   ntrack i32[W]         1: the slot's list is exact; 0: not kept (core);
-//                         2: not kept, queued for a rebuild
-//   relist i32[2W]        slots queued for a list rebuild this slide
+//   ntrack i32[W]         1: the slot's list is exact; 0: not kept (core, or
+//                         rebuilt at the end of the slide)
 //   chunk scratch: sort words, expired points.
 #pragma once
 
@@ -63,7 +62,7 @@ struct Ctl {
     int nitems;                // work items of the current grid
     int ncells;                // cells of the current grid
     int err;                   // kErr* bits
-    int relist_n;              // slots queued in View::relist this slide
+    int pad0;
     int union_next;            // next work item handed out by k_union
     int label_next;            // next work item handed out by k_label
     unsigned long long band_rechecks;
@@ -111,8 +110,7 @@ struct View {
     int* cid;
     int* nlist;                  // [W][list_stride] neighbours of non-core points
     int* rslot;                  // per slot: root of a core, -1 otherwise
-    int* ntrack;                 // per slot: list state (1 exact, 0 not kept, 2 queued)
-    int* relist;                 // [2W] slots whose lists are rebuilt this slide
+    int* ntrack;                 // per slot: 1 list exact, 0 not kept
     unsigned long long* nsort;   // chunk sort words in (key << 14 | offset)
     unsigned long long* xsort;
     unsigned long long* nword;   // sorted

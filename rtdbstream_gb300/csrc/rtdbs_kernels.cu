@@ -337,9 +337,10 @@ __device__ __forceinline__ void flush_stats(const View& v, const Tally& t, int e
 // besides itself) in a fixed list by slot, maintained from the same distance
 // tests that keep the counts exact: an expired neighbour is removed in the
 // decrement pass, a new one appended in the increment pass.  A point that
-// becomes core stops keeping its list (ntrack 0); one that drops back below
-// MinPts is queued and its list rebuilt by one scan once the slide's counts
-// are final.  The label pass then reads lists instead of scanning the grid.
+// becomes core stops keeping its list (ntrack 0); one that is below MinPts
+// without a list once the slide's counts are final (it lost core status) gets
+// its list rebuilt by one scan.  The label pass then reads lists instead of
+// scanning the grid.
 
 // Appends slot p to q's list (q tracked); a full list means q has reached
 // MinPts, so it stops being kept.
@@ -361,16 +362,6 @@ __device__ __forceinline__ void list_remove(const View& v, int q, int p) {
     atomicOr(&v.ctl->err, kErrList);
 }
 
-// Queues slot q (just fell below MinPts, list not kept) for a rebuild, once.
-__device__ __forceinline__ void relist_push(const View& v, int q) {
-    if (atomicCAS(&v.ntrack[q], 0, 2) != 0) return;
-    const int at = atomicAdd(&v.ctl->relist_n, 1);
-    if (at < 2 * v.W)
-        v.relist[at] = q;
-    else
-        atomicOr(&v.ctl->err, kErrList);
-}
-
 // Warp-wide: adds the lanes' neighbour slots (nb) to the warp's buffer in
 // lane order; returns the new number found (entries past cap are dropped,
 // the list is then not kept anyway).
@@ -387,7 +378,8 @@ __device__ __forceinline__ void list_store(const View& v, int a, int nfound, con
     __syncwarp();
     const bool keep = nfound + 1 < v.min_pts;
     int* L = v.nlist + (size_t)a * v.list_stride;
-    for (int k = lane; k < v.list_stride; k += 32) L[k] = (keep && k < nfound) ? buf[k] : -1;
+    if (keep)
+        for (int k = lane; k < v.list_stride; k += 32) L[k] = k < nfound ? buf[k] : -1;
     if (lane == 0) v.ntrack[a] = keep ? 1 : 0;
     __syncwarp();
 }
@@ -558,6 +550,8 @@ __global__ void __launch_bounds__(kSortRun) k_runmerge(View v, int c, int init) 
 struct StreamSmem {
     int rstart[8][9], rpre[8][10];
     int nbuf[8][kListCap];
+    int queue[256];  // k_relist: positions to rebuild in the block's range
+    int nq;
 };
 
 template <int MODE, int DIM>
@@ -586,15 +580,11 @@ __device__ __forceinline__ void decr_body(const View& v, int j, int c, int bx, S
     for (int idx = lane; idx < total; idx += 32) {
         const int pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
         const float4 q = spt[pos];
+        const int cnt = scnt[pos];  // counts only fall here: >= MinPts means no list kept
         const int qs = slot_of(q);
         if ((qs < el || qs >= el + c) && is_nbr<MODE, DIM>(v, xp, q, tally)) {
-            const int was = atomicSub(&scnt[pos], 1);
-            if (lists) {
-                if (was == v.min_pts)
-                    relist_push(v, qs);
-                else if (was < v.min_pts && v.ntrack[qs] == 1)
-                    list_remove(v, qs, xs);
-            }
+            atomicSub(&scnt[pos], 1);
+            if (lists && cnt < v.min_pts && v.ntrack[qs] == 1) list_remove(v, qs, xs);
         }
     }
     flush_stats(v, tally, 0, lane);
@@ -880,6 +870,7 @@ __device__ __forceinline__ void incr_body(const View& v, int j, int c, int init,
         if (idx < total) {
             const int pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
             const float4 q = spt[pos];
+            const int cnt = scnt[pos];  // counts only rise here: >= MinPts means no list kept
             qs = slot_of(q);
             if (qs == aslot) {
                 ++count;
@@ -889,7 +880,7 @@ __device__ __forceinline__ void incr_body(const View& v, int j, int c, int init,
                 nb = true;
                 if (qs < el || qs >= el + c) {
                     atomicAdd(&scnt[pos], 1);
-                    if (lists && v.ntrack[qs] == 1) list_append(v, qs, aslot);
+                    if (lists && cnt < v.min_pts && v.ntrack[qs] == 1) list_append(v, qs, aslot);
                 }
             }
         }
@@ -1149,8 +1140,10 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advanc
     label_body<MODE, DIM>(v, advance, blockIdx.x, sm);
 }
 
-// Rebuilds the lists of the queued slots (points that fell below MinPts this
-// slide) from one scan of the final grid; warp per queued slot.
+// Rebuilds the list of every point below MinPts without one (it lost core
+// status this slide) from one scan of the final grid.  Each block checks a
+// range of sorted positions, queues the points it finds in shared memory and
+// rebuilds them warp by warp.
 template <int MODE, int DIM>
 __device__ __forceinline__ void relist_body(const View& v, int bx, int nbx, StreamSmem& sm) {
     int(&rstart)[8][9] = sm.rstart;
@@ -1159,29 +1152,43 @@ __device__ __forceinline__ void relist_body(const View& v, int bx, int nbx, Stre
     const long long b = v.ctl->b;
     const int cur = (int)(b & 1);
     const unsigned gen = gen_of_build(b);
-    const int n = min(v.ctl->relist_n, 2 * v.W);
+    const int n = v.ctl->nocc[cur];
     const float4* spt = v.spt[cur];
+    const int* scnt = v.scnt[cur];
     int* nbuf = sm.nbuf[wib];
     Tally tally;
-    for (int e = bx * wpb + wib; e < n; e += nbx * wpb) {
-        const int a = v.relist[e];
-        const float4 ap = v.ring[a];
-        int rs, re;
-        row_ranges<DIM, false>(v, v.table[cur], gen, v.kslot[a], lane, rs, re);
-        const int total = candidate_stream<Stencil<DIM, false>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
-        int r = 0, nfound = 0;
-        for (int base = 0; base < total; base += 32) {
-            const int idx = base + lane;
-            bool nb = false;
-            int qs = -1;
-            if (idx < total) {
-                const float4 q = spt[stream_pos(idx, r, rstart[wib], rpre[wib])];
-                qs = slot_of(q);
-                nb = qs != a && is_nbr<MODE, DIM>(v, ap, q, tally);
-            }
-            nfound = list_collect(nb, qs, nfound, v.list_cap, nbuf, lane);
+    for (int p0 = bx * blockDim.x; p0 < n; p0 += nbx * blockDim.x) {
+        __syncthreads();
+        if (threadIdx.x == 0) sm.nq = 0;
+        __syncthreads();
+        const int i = p0 + threadIdx.x;
+        if (i < n && scnt[i] < v.min_pts) {
+            const int slot = slot_of(spt[i]);
+            if (v.ntrack[slot] != 1) sm.queue[atomicAdd(&sm.nq, 1)] = i;
         }
-        list_store(v, a, nfound, nbuf, lane);
+        __syncthreads();
+        const int nq = sm.nq;
+        for (int e = wib; e < nq; e += wpb) {
+            const int at = sm.queue[e];
+            const float4 ap = spt[at];
+            const int a = slot_of(ap);
+            int rs, re;
+            row_ranges<DIM, false>(v, v.table[cur], gen, v.skey[cur][at], lane, rs, re);
+            const int total = candidate_stream<Stencil<DIM, false>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
+            int r = 0, nfound = 0;
+            for (int base = 0; base < total; base += 32) {
+                const int idx = base + lane;
+                bool nb = false;
+                int qs = -1;
+                if (idx < total) {
+                    const float4 q = spt[stream_pos(idx, r, rstart[wib], rpre[wib])];
+                    qs = slot_of(q);
+                    nb = qs != a && is_nbr<MODE, DIM>(v, ap, q, tally);
+                }
+                nfound = list_collect(nb, qs, nfound, v.list_cap, nbuf, lane);
+            }
+            list_store(v, a, nfound, nbuf, lane);
+        }
     }
     flush_stats(v, tally, 0, lane);
 }
@@ -1223,7 +1230,6 @@ __device__ __forceinline__ void border_body(const View& v, int advance, int bx, 
     }
     if (bx == 0 && threadIdx.x == 0) {
         v.ctl->union_next = 0;                // the next clustering's queue; not read here
-        v.ctl->relist_n = 0;                  // rebuilds done
         if (advance) v.ctl->slide += 1;       // no reader here
     }
 }
@@ -1258,10 +1264,10 @@ struct PhaseShape;
 template <> struct PhaseShape<kBatchIngest> { static constexpr int threads = 256, min_blocks = 1; };
 template <> struct PhaseShape<kBatchSort> { static constexpr int threads = kSortRun, min_blocks = 1; };
 template <> struct PhaseShape<kBatchRunmerge> { static constexpr int threads = kSortRun, min_blocks = 1; };
-template <> struct PhaseShape<kBatchDecrement> { static constexpr int threads = 256, min_blocks = 1; };
+template <> struct PhaseShape<kBatchDecrement> { static constexpr int threads = 256, min_blocks = 8; };
 template <> struct PhaseShape<kBatchMerge> { static constexpr int threads = kMergeThreads, min_blocks = 1; };
 template <> struct PhaseShape<kBatchBuild> { static constexpr int threads = kBuildThreads, min_blocks = 1; };
-template <> struct PhaseShape<kBatchIncrement> { static constexpr int threads = 256, min_blocks = 1; };
+template <> struct PhaseShape<kBatchIncrement> { static constexpr int threads = 256, min_blocks = 8; };
 template <> struct PhaseShape<kBatchUnion> { static constexpr int threads = kClusterThreads, min_blocks = 8; };
 template <> struct PhaseShape<kBatchFlatten> { static constexpr int threads = 256, min_blocks = 1; };
 template <> struct PhaseShape<kBatchRelist> { static constexpr int threads = 256, min_blocks = 1; };
@@ -1405,7 +1411,7 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
         case kPhaseLabel:
             if (v.list_cap >= 0) {
                 const int sms = g_num_sms > 0 ? g_num_sms : 152;
-                RTDBS_DISPATCH(precision, v.dim, k_relist, sms, 256, s, v);
+                RTDBS_DISPATCH(precision, v.dim, k_relist, max(1, min(sms * 8, (v.W + 255) / 256)), 256, s, v);
                 k_border<<<max(1, min(sms * 8, (v.W + 255) / 256)), 256, 0, s>>>(v, advance);
                 break;
             }
@@ -1476,7 +1482,7 @@ int batch_blocks(int phase, const View& v, int c) {
             if (v.list_cap >= 0) return max(1, min(1024, (v.W + 1023) / 1024));  // k_border
             return max(1, min(1024, (v.W + 4095) / 4096));  // persistent, queue-fed
         case kBatchFlatten: return max(1, min(1024, (v.W + 2047) / 2048));
-        case kBatchRelist: return v.list_cap >= 0 ? max(1, min(64, (v.W + 16383) / 16384)) : 0;
+        case kBatchRelist: return v.list_cap >= 0 ? max(1, min(1024, (v.W + 255) / 256)) : 0;
         default: return 0;
     }
 }
