@@ -1477,7 +1477,7 @@ int batch_blocks(int phase, const View& v, int c) {
         case kBatchIncrement: return (c * 32 + 255) / 256;
         case kBatchMerge: return (v.W + kMergeTile - 1) / kMergeTile;
         case kBatchBuild: return (v.W + kBuildThreads - 1) / kBuildThreads;
-        case kBatchUnion:
+        case kBatchUnion: return max(1, min(1024, (v.W + 1023) / 1024));  // persistent, queue-fed
         case kBatchLabel:
             if (v.list_cap >= 0) return max(1, min(1024, (v.W + 1023) / 1024));  // k_border
             return max(1, min(1024, (v.W + 4095) / 4096));  // persistent, queue-fed
