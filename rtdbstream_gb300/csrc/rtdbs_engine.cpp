@@ -550,8 +550,7 @@ int rtdbs_get_stats(rtdbs_engine* e, rtdbs_stats* s) {
     s->device_bytes = (int64_t)e->dev_bytes;
     const int nchunks = (e->p.stride + e->chunk - 1) / e->chunk;
     s->chunks_per_slide = nchunks;
-    // sort phase = 2 kernels; label phase = relist + border with neighbour lists
-    s->launches_per_slide = nchunks * (rtdbs::kChunkPhases + 1) + (e->v.list_cap >= 0 ? 4 : 3);
+    s->launches_per_slide = nchunks * (rtdbs::kChunkPhases + 1) + 3;  // sort phase = 2 kernels
     return RTDBS_OK;
 }
 
@@ -1051,8 +1050,7 @@ int rtdbs_pool_slide_profiled(rtdbs_pool* p, int32_t n, const int32_t* ids, cons
     if (rc == RTDBS_OK) rc = rtdbs_pool_sync(p);
     if (rc == RTDBS_OK) {
         // batch phases -> the engine's phase slots (sort + run merge are one)
-        // (the list rebuild belongs to the label phase, as in the single-stream launch)
-        static const int slot[rtdbs::kNumBatchPhases] = {0, 1, 1, 2, 3, 4, 5, 6, 7, 8, 8};
+        static const int slot[rtdbs::kNumBatchPhases] = {0, 1, 1, 2, 3, 4, 5, 6, 7, 8};
         float ph[9] = {0};
         for (size_t i = 0; i < p->plan.size(); ++i) {
             float ms = 0.f;

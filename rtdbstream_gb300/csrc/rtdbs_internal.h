@@ -161,7 +161,6 @@ enum BatchPhase : int {
     kBatchIncrement,
     kBatchUnion,
     kBatchFlatten,
-    kBatchRelist,
     kBatchLabel,
     kNumBatchPhases
 };

@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(kSortRun) k_runmerge(View v, int c, int init) 
 struct StreamSmem {
     int rstart[8][9], rpre[8][10];
     int nbuf[8][kListCap];
-    int queue[256];  // k_relist: positions to rebuild in the block's range
+    int queue[256];  // k_flatten: positions whose lists are rebuilt, in the block's tile
     int nq;
 };
 
@@ -1025,23 +1025,76 @@ __global__ void __launch_bounds__(kClusterThreads, 8) k_union(View v) {
 // Root of every core point, walked from the position's root hint.  Without
 // neighbour lists: by sorted position (-1 for non-core points), for the grid
 // scan of k_label.  With lists: by slot (rslot), which k_border turns into
-// the outputs.
-__device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx) {
+// the outputs; and a point below MinPts without a list (it lost core status
+// this slide) gets its list rebuilt here from one scan of the final grid --
+// each block queues such points of its 256-position tile in shared memory
+// and rebuilds them warp by warp.
+template <int MODE, int DIM>
+__device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx, StreamSmem& sm) {
     if (bx == 0 && threadIdx.x == 0) v.ctl->label_next = 0;  // k_label's queue; not read here
-    const int cur = (int)(v.ctl->b & 1);
+    const long long b = v.ctl->b;
+    const int cur = (int)(b & 1);
     const int n = v.ctl->nocc[cur];
     const int* scnt = v.scnt[cur];
-    if (v.list_cap >= 0) {
-        const int* sw = reinterpret_cast<const int*>(v.spt[cur]) + 3;  // .w = slot
+    if (v.list_cap < 0) {
         for (int i = bx * blockDim.x + threadIdx.x; i < n; i += nbx * blockDim.x)
-            v.rslot[sw[4 * (size_t)i]] = scnt[i] >= v.min_pts ? uf_find(v.parent, v.sroot[i]) : -1;
+            v.sroot[i] = scnt[i] >= v.min_pts ? uf_find(v.parent, v.sroot[i]) : -1;
         return;
     }
-    for (int i = bx * blockDim.x + threadIdx.x; i < n; i += nbx * blockDim.x)
-        v.sroot[i] = scnt[i] >= v.min_pts ? uf_find(v.parent, v.sroot[i]) : -1;
+    int(&rstart)[8][9] = sm.rstart;
+    int(&rpre)[8][10] = sm.rpre;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const unsigned gen = gen_of_build(b);
+    const float4* spt = v.spt[cur];
+    const int* sw = reinterpret_cast<const int*>(spt) + 3;  // .w = slot
+    int* nbuf = sm.nbuf[wib];
+    Tally tally;
+    for (int p0 = bx * blockDim.x; p0 < n; p0 += nbx * blockDim.x) {
+        __syncthreads();
+        if (threadIdx.x == 0) sm.nq = 0;
+        __syncthreads();
+        const int i = p0 + threadIdx.x;
+        if (i < n) {
+            const int slot = sw[4 * (size_t)i];
+            if (scnt[i] >= v.min_pts) {
+                v.rslot[slot] = uf_find(v.parent, v.sroot[i]);
+            } else {
+                v.rslot[slot] = -1;
+                if (v.ntrack[slot] != 1) sm.queue[atomicAdd(&sm.nq, 1)] = i;
+            }
+        }
+        __syncthreads();
+        const int nq = sm.nq;
+        for (int e = wib; e < nq; e += wpb) {
+            const int at = sm.queue[e];
+            const float4 ap = spt[at];
+            const int a = slot_of(ap);
+            int rs, re;
+            row_ranges<DIM, false>(v, v.table[cur], gen, v.skey[cur][at], lane, rs, re);
+            const int total = candidate_stream<Stencil<DIM, false>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
+            int r = 0, nfound = 0;
+            for (int base = 0; base < total; base += 32) {
+                const int idx = base + lane;
+                bool nb = false;
+                int qs = -1;
+                if (idx < total) {
+                    const float4 q = spt[stream_pos(idx, r, rstart[wib], rpre[wib])];
+                    qs = slot_of(q);
+                    nb = qs != a && is_nbr<MODE, DIM>(v, ap, q, tally);
+                }
+                nfound = list_collect(nb, qs, nfound, v.list_cap, nbuf, lane);
+            }
+            list_store(v, a, nfound, nbuf, lane);
+        }
+    }
+    flush_stats(v, tally, 0, lane);
 }
 
-__global__ void k_flatten(View v) { flatten_body(v, blockIdx.x, gridDim.x); }
+template <int MODE, int DIM>
+__global__ void __launch_bounds__(256) k_flatten(View v) {
+    __shared__ StreamSmem sm;
+    flatten_body<MODE, DIM>(v, blockIdx.x, gridDim.x, sm);
+}
 
 // Labels and ids by slot: core -> 0 and its root; non-core -> 1 and the
 // minimum root over adjacent cores, or 2 and its own slot.
@@ -1140,65 +1193,6 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advanc
     label_body<MODE, DIM>(v, advance, blockIdx.x, sm);
 }
 
-// Rebuilds the list of every point below MinPts without one (it lost core
-// status this slide) from one scan of the final grid.  Each block checks a
-// range of sorted positions, queues the points it finds in shared memory and
-// rebuilds them warp by warp.
-template <int MODE, int DIM>
-__device__ __forceinline__ void relist_body(const View& v, int bx, int nbx, StreamSmem& sm) {
-    int(&rstart)[8][9] = sm.rstart;
-    int(&rpre)[8][10] = sm.rpre;
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-    const long long b = v.ctl->b;
-    const int cur = (int)(b & 1);
-    const unsigned gen = gen_of_build(b);
-    const int n = v.ctl->nocc[cur];
-    const float4* spt = v.spt[cur];
-    const int* scnt = v.scnt[cur];
-    int* nbuf = sm.nbuf[wib];
-    Tally tally;
-    for (int p0 = bx * blockDim.x; p0 < n; p0 += nbx * blockDim.x) {
-        __syncthreads();
-        if (threadIdx.x == 0) sm.nq = 0;
-        __syncthreads();
-        const int i = p0 + threadIdx.x;
-        if (i < n && scnt[i] < v.min_pts) {
-            const int slot = slot_of(spt[i]);
-            if (v.ntrack[slot] != 1) sm.queue[atomicAdd(&sm.nq, 1)] = i;
-        }
-        __syncthreads();
-        const int nq = sm.nq;
-        for (int e = wib; e < nq; e += wpb) {
-            const int at = sm.queue[e];
-            const float4 ap = spt[at];
-            const int a = slot_of(ap);
-            int rs, re;
-            row_ranges<DIM, false>(v, v.table[cur], gen, v.skey[cur][at], lane, rs, re);
-            const int total = candidate_stream<Stencil<DIM, false>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
-            int r = 0, nfound = 0;
-            for (int base = 0; base < total; base += 32) {
-                const int idx = base + lane;
-                bool nb = false;
-                int qs = -1;
-                if (idx < total) {
-                    const float4 q = spt[stream_pos(idx, r, rstart[wib], rpre[wib])];
-                    qs = slot_of(q);
-                    nb = qs != a && is_nbr<MODE, DIM>(v, ap, q, tally);
-                }
-                nfound = list_collect(nb, qs, nfound, v.list_cap, nbuf, lane);
-            }
-            list_store(v, a, nfound, nbuf, lane);
-        }
-    }
-    flush_stats(v, tally, 0, lane);
-}
-
-template <int MODE, int DIM>
-__global__ void __launch_bounds__(256) k_relist(View v) {
-    __shared__ StreamSmem sm;
-    relist_body<MODE, DIM>(v, blockIdx.x, gridDim.x, sm);
-}
-
 // Outputs by slot from the roots and the lists: core -> 0 and its root; a
 // non-core point with a core neighbour -> 1 and the minimum root over its
 // core neighbours; else noise -> 2 and its own slot.  Ends the slide like
@@ -1270,7 +1264,6 @@ template <> struct PhaseShape<kBatchBuild> { static constexpr int threads = kBui
 template <> struct PhaseShape<kBatchIncrement> { static constexpr int threads = 256, min_blocks = 8; };
 template <> struct PhaseShape<kBatchUnion> { static constexpr int threads = kClusterThreads, min_blocks = 8; };
 template <> struct PhaseShape<kBatchFlatten> { static constexpr int threads = 256, min_blocks = 1; };
-template <> struct PhaseShape<kBatchRelist> { static constexpr int threads = 256, min_blocks = 1; };
 template <> struct PhaseShape<kBatchLabel> { static constexpr int threads = kClusterThreads, min_blocks = 6; };
 
 // One phase over many streams.  The block finds its item, copies that
@@ -1329,10 +1322,8 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
         __shared__ ClusterSmem sm;
         RTDBS_BODY_DISPATCH(prec, dim, union_body, sv, sm);
     } else if constexpr (PHASE == kBatchFlatten) {
-        flatten_body(sv, bx, nbx);
-    } else if constexpr (PHASE == kBatchRelist) {
         __shared__ StreamSmem sm;
-        if (sv.list_cap >= 0) RTDBS_BODY_DISPATCH(prec, dim, relist_body, sv, bx, nbx, sm);
+        RTDBS_BODY_DISPATCH(prec, dim, flatten_body, sv, bx, nbx, sm);
     } else {
         __shared__ ClusterSmem sm;
         if (sv.list_cap >= 0)
@@ -1411,7 +1402,6 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
         case kPhaseLabel:
             if (v.list_cap >= 0) {
                 const int sms = g_num_sms > 0 ? g_num_sms : 152;
-                RTDBS_DISPATCH(precision, v.dim, k_relist, max(1, min(sms * 8, (v.W + 255) / 256)), 256, s, v);
                 k_border<<<max(1, min(sms * 8, (v.W + 255) / 256)), 256, 0, s>>>(v, advance);
                 break;
             }
@@ -1429,7 +1419,7 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
         }
         case kPhaseFlatten: {
             const int sms = g_num_sms > 0 ? g_num_sms : 152;
-            k_flatten<<<sms * 8, 256, 0, s>>>(v);
+            RTDBS_DISPATCH(precision, v.dim, k_flatten, sms * 8, 256, s, v);
             break;
         }
         default:
@@ -1482,7 +1472,6 @@ int batch_blocks(int phase, const View& v, int c) {
             if (v.list_cap >= 0) return max(1, min(1024, (v.W + 1023) / 1024));  // k_border
             return max(1, min(1024, (v.W + 4095) / 4096));  // persistent, queue-fed
         case kBatchFlatten: return max(1, min(1024, (v.W + 2047) / 2048));
-        case kBatchRelist: return v.list_cap >= 0 ? max(1, min(1024, (v.W + 255) / 256)) : 0;
         default: return 0;
     }
 }
@@ -1503,7 +1492,6 @@ cudaError_t launch_batch(int phase, const BatchLaunch& L, int total_blocks, int 
         case kBatchIncrement: k_batch<kBatchIncrement><<<total_blocks, t, 0, s>>>(L); break;
         case kBatchUnion: k_batch<kBatchUnion><<<total_blocks, t, 0, s>>>(L); break;
         case kBatchFlatten: k_batch<kBatchFlatten><<<total_blocks, t, 0, s>>>(L); break;
-        case kBatchRelist: k_batch<kBatchRelist><<<total_blocks, t, 0, s>>>(L); break;
         case kBatchLabel: k_batch<kBatchLabel><<<total_blocks, t, 0, s>>>(L); break;
         default: return cudaErrorInvalidValue;
     }
