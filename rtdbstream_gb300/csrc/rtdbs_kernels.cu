@@ -638,6 +638,9 @@ __device__ __forceinline__ void merge_body(const View& v, int j, int c, int init
     const int n_new = n_old - (init ? 0 : c) + c;
     const int el = chunk_base_slot(v, j, init);
     const int tid = threadIdx.x;
+    // a fresh union-find forest: with neighbour lists k_border resets it by
+    // slot at the end of every clustering, so only the first window needs it
+    const bool reset_parent = init || v.list_cap < 0;
     if (bx == 0 && tid == 0) {
         v.ctl->nocc[dst] = n_new;
         v.ctl->nitems = 0;
@@ -735,7 +738,7 @@ __device__ __forceinline__ void merge_body(const View& v, int j, int c, int init
         dpt[o] = opt[ts + i];
         dcnt[o] = ocnt[ts + i];
         v.sroot[o] = s;
-        v.parent[s] = s;
+        if (reset_parent) v.parent[s] = s;
     }
     // new entries of this tile
     for (int q = jt0 + tid; q < jt1; q += kMergeThreads) {
@@ -759,7 +762,7 @@ __device__ __forceinline__ void merge_body(const View& v, int j, int c, int init
         dpt[o] = v.ring[slot];
         dcnt[o] = 0;
         v.sroot[o] = slot;
-        v.parent[slot] = slot;
+        if (reset_parent) v.parent[slot] = slot;
     }
 }
 
@@ -1195,8 +1198,9 @@ __global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advanc
 
 // Outputs by slot from the roots and the lists: core -> 0 and its root; a
 // non-core point with a core neighbour -> 1 and the minimum root over its
-// core neighbours; else noise -> 2 and its own slot.  Ends the slide like
-// k_label.
+// core neighbours; else noise -> 2 and its own slot.  Resets the union-find
+// forest for the next clustering (coalesced, by slot) and ends the slide
+// like k_label.
 __device__ __forceinline__ void border_body(const View& v, int advance, int bx, int nbx) {
     for (int s = bx * blockDim.x + threadIdx.x; s < v.W; s += nbx * blockDim.x) {
         const int root = v.rslot[s];
@@ -1221,6 +1225,7 @@ __device__ __forceinline__ void border_body(const View& v, int advance, int bx, 
         }
         v.label[s] = lab;
         v.cid[s] = id;
+        v.parent[s] = s;
     }
     if (bx == 0 && threadIdx.x == 0) {
         v.ctl->union_next = 0;                // the next clustering's queue; not read here
