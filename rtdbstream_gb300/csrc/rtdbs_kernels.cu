@@ -616,14 +616,47 @@ __device__ __forceinline__ int count_words_less(const unsigned long long* words,
     return lo;
 }
 
+// Warp-wide count of sorted words below (key, slot): a 32-way search, one
+// dependent load per factor-32 narrowing (3 rounds for a 16384-word chunk).
+__device__ __forceinline__ int warp_count_words_less(const unsigned long long* words, int n, int el,
+                                                     unsigned long long key, int slot, int lane) {
+    int lo = 0, hi = n;  // words below lo are less, words from hi on are not
+    while (hi - lo > 32) {
+        const int step = (hi - lo + 31) >> 5;
+        const int piv = lo + lane * step;
+        bool less = false;
+        if (piv < hi) {
+            const unsigned long long w = words[piv];
+            less = tuple_less(w >> kOffBits, el + (int)(w & ((1u << kOffBits) - 1)), key, slot);
+        }
+        const int c = __popc(__ballot_sync(kFull, less));
+        if (c == 0) {
+            hi = lo;
+            break;
+        }
+        const int nlo = lo + (c - 1) * step + 1;
+        hi = min(hi, lo + c * step);
+        lo = nlo;
+    }
+    bool less = false;
+    if (lo + lane < hi) {
+        const unsigned long long w = words[lo + lane];
+        less = tuple_less(w >> kOffBits, el + (int)(w & ((1u << kOffBits) - 1)), key, slot);
+    }
+    return lo + __popc(__ballot_sync(kFull, less));
+}
+
 // Old sorted window minus the expired slots [el, el+c), merged with the c
 // new entries; tile t of the old window goes to output offset
 // ts - (#expired before ts) + (#new before old[ts]).
+constexpr int kMergeStage = 1024;  // new words of a tile staged in shared memory
 struct MergeSmem {
     unsigned long long tkey[kMergeTile];
+    unsigned long long nw[kMergeStage];
     int tslot[kMergeTile];
     int spre[kMergeTile + 1];
     unsigned wsum[32];
+    int bnd[3];
 };
 
 __device__ __forceinline__ void merge_body(const View& v, int j, int c, int init, int bx, int nbx,
@@ -667,22 +700,33 @@ __device__ __forceinline__ void merge_body(const View& v, int j, int c, int init
     float4* dpt = v.spt[dst];
     int* dcnt = v.scnt[dst];
 
-    int jt0 = 0, jt1 = c, e0 = 0;
-    if (tlen > 0) {
-        const unsigned long long k0 = okey[ts];
-        const int s0 = slot_of(opt[ts]);
-        if (t > 0) jt0 = count_words_less(v.nword, c, el, k0, s0);
-        if (!init) e0 = count_words_less(v.xword, c, el, k0, s0);
-        if (t < ntiles - 1) jt1 = count_words_less(v.nword, c, el, okey[te], slot_of(opt[te]));
+    // tile bounds among the new / expired words: warps 0, 1, 2 search at once
+    {
+        const int lane = tid & 31, w = tid >> 5;
+        if (w < 3) {
+            const bool need = tlen > 0 && (w == 0 ? t > 0 : (w == 1 ? !init : t < ntiles - 1));
+            int r = w == 2 ? c : 0;
+            if (need) {
+                const int at = w == 2 ? te : ts;
+                r = warp_count_words_less(w == 1 ? v.xword : v.nword, c, el, okey[at], slot_of(opt[at]),
+                                          lane);
+            }
+            if (lane == 0) sm.bnd[w] = r;
+        }
     }
-    const int base = ts - e0 + jt0;
-
     // tile -> shared memory; survivor prefix in item order
     for (int i = tid; i < tlen; i += kMergeThreads) {
         tkey[i] = okey[ts + i];
         tslot[i] = slot_of(opt[ts + i]);
     }
     __syncthreads();
+    const int jt0 = sm.bnd[0], e0 = sm.bnd[1], jt1 = sm.bnd[2];
+    const int base = ts - e0 + jt0;
+    const int m = jt1 - jt0;
+    const bool staged = m <= kMergeStage;
+    const unsigned long long* nw = staged ? sm.nw : v.nword + jt0;  // the tile's new words
+    if (staged)
+        for (int i = tid; i < m; i += kMergeThreads) sm.nw[i] = v.nword[jt0 + i];
     unsigned flags[4];
     unsigned cnt = 0;
 #pragma unroll
@@ -724,11 +768,10 @@ __device__ __forceinline__ void merge_body(const View& v, int j, int c, int init
     __syncthreads();
 
     // survivors (coalesced, item order i = tid + 256 k)
-    const int m = jt1 - jt0;
     for (int i = tid; i < tlen; i += kMergeThreads) {
         const int s = tslot[i];
         if (!(init || s < el || s >= el + c)) continue;
-        const int lessnew = m > 0 ? count_words_less(v.nword + jt0, m, el, tkey[i], s) : 0;
+        const int lessnew = m > 0 ? count_words_less(nw, m, el, tkey[i], s) : 0;
         const int o = base + spre[i] + lessnew;
         if (o < 0 || o >= n_new) {
             atomicOr(&v.ctl->err, kErrChunk);
@@ -742,7 +785,7 @@ __device__ __forceinline__ void merge_body(const View& v, int j, int c, int init
     }
     // new entries of this tile
     for (int q = jt0 + tid; q < jt1; q += kMergeThreads) {
-        const unsigned long long wd = v.nword[q];
+        const unsigned long long wd = nw[q - jt0];
         const unsigned long long key = wd >> kOffBits;
         const int slot = el + (int)(wd & ((1u << kOffBits) - 1));
         int lo = 0, hi = tlen;  // old tile entries below (key, slot)
