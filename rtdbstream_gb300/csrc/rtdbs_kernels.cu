@@ -161,26 +161,30 @@ __device__ __forceinline__ int2 table_find(const ulonglong2* T, unsigned pmask, 
 }
 
 // Claims (or finds) the slot of `tag` and stores one half of its range:
-// which = 0 -> start, 1 -> end.  Entries of older generations count as free.
+// which = 0 -> start, 1 -> end, 2 -> both (value = start, value2 = end).
+// Entries of older generations count as free.
 __device__ bool table_set(ulonglong2* T, unsigned pmask, int pbits, unsigned long long tag,
-                          int which, int value) {
+                          int which, int value, int value2 = 0) {
     unsigned s = table_home(tag & kKeyMask, pbits);
     const unsigned long long gen = tag >> kKeyBitsMax;
     for (unsigned i = 0; i <= pmask; ++i) {
         unsigned long long* kp = reinterpret_cast<unsigned long long*>(&T[s].x);
         unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(kp);
         for (int t = 0; t < 8; ++t) {
-            if (cur == tag) {
-                reinterpret_cast<int*>(&T[s].y)[which] = value;
+            bool mine = cur == tag;
+            if (!mine) {
+                if ((cur >> kKeyBitsMax) == gen) break;  // another cell of this generation
+                const unsigned long long prev = atomicCAS(kp, cur, tag);
+                mine = prev == cur;
+                cur = prev;
+            }
+            if (mine) {
+                if (which == 2)
+                    T[s].y = (unsigned long long)(unsigned)value | ((unsigned long long)(unsigned)value2 << 32);
+                else
+                    reinterpret_cast<int*>(&T[s].y)[which] = value;
                 return true;
             }
-            if ((cur >> kKeyBitsMax) == gen) break;  // another cell of this generation
-            const unsigned long long prev = atomicCAS(kp, cur, tag);
-            if (prev == cur) {
-                reinterpret_cast<int*>(&T[s].y)[which] = value;
-                return true;
-            }
-            cur = prev;
         }
         s = (s + 1) & pmask;
     }
@@ -846,8 +850,18 @@ __device__ __forceinline__ void build_body(const View& v, int bx, BuildSmem& sm)
     int err = 0;
     ulonglong2* T = v.table[cur];
     const unsigned long long tag = tag_of(k & kKeyMask, gen);
-    if (first && !table_set(T, v.pmask, v.pbits, tag, 0, i)) err |= kErrHashFull;
-    if (last && !table_set(T, v.pmask, v.pbits, tag, 1, i + 1)) err |= kErrHashFull;
+    // A cell that starts and ends in this warp is entered once, by its first
+    // point; otherwise its first point enters the start, its last the end.
+    const unsigned firsts = __ballot_sync(kFull, first);
+    const unsigned lasts = __ballot_sync(kFull, last);
+    if (first) {
+        const unsigned ends = lasts & ~((1u << lane) - 1u);  // my cell's last is the lowest
+        const bool ok = ends ? table_set(T, v.pmask, v.pbits, tag, 2, i, gw * 32 + __ffs(ends))
+                             : table_set(T, v.pmask, v.pbits, tag, 0, i);
+        if (!ok) err |= kErrHashFull;
+    }
+    if (last && !(firsts & ((2u << lane) - 1u)) && !table_set(T, v.pmask, v.pbits, tag, 1, i + 1))
+        err |= kErrHashFull;
     const unsigned starts = __ballot_sync(kFull, valid && (first || lane == 0));
     const int nfirst = __popc(__ballot_sync(kFull, first));
     if (threadIdx.x == 0) bcells = 0;
