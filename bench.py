@@ -230,8 +230,10 @@ def algorithmic_bytes(phase: str, W: int, S: int, dim: int, cells: int, items: i
         "build": W * 8 + cells * 32 + items * 8,
         "increment": c * (8 + 16) + c * 4,
         "union": W * (16 + 4 + 4 + 4),
-        "flatten": W * (16 + 4 + 4 + 4),
-        "label": W * (16 + 4 + 8),
+        # scnt, slot, root hint, parent read; root by slot written
+        "flatten": W * (4 + 4 + 4 + 4 + 4),
+        # border pass: root by slot read; label, cid, parent written
+        "label": W * (4 + 4 + 4 + 4),
     }[phase]
 
 
@@ -251,7 +253,7 @@ def ncu_traffic(phase: str):
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get(f"k_{phase}")
+            return json.load(f).get({"label": "k_border"}.get(phase, f"k_{phase}"))
     except (OSError, ValueError):
         return None
 
