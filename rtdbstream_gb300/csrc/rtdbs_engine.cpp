@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -659,7 +660,7 @@ struct rtdbs_pool {
     cudaGraphExec_t graph = nullptr;
     // launch plan of the cached shape
     struct Launch {
-        int phase;
+        int phase, prec, dim;          // prec/dim: the stream group of a split phase
         size_t items_off, prefix_off;  // byte offsets into d_tables
         int n, blocks, max_c;
     };
@@ -709,6 +710,37 @@ int pool_build_shape(rtdbs_pool* p, const std::vector<int>& ids) {
         return at;
     };
     std::vector<rtdbs_pool::Launch> plan;
+    // One launch of phase ph over `items`; split phases get one launch per
+    // (precision, dim) group present.
+    auto add_launches = [&](int ph, const std::vector<BatchItem>& items) {
+        std::vector<std::pair<int, int>> groups;
+        if (rtdbs::batch_phase_split(ph)) {
+            for (const auto& it : items) {
+                const auto& v = p->eng[it.view]->v;
+                const std::pair<int, int> g(v.precision, v.dim);
+                if (std::find(groups.begin(), groups.end(), g) == groups.end()) groups.push_back(g);
+            }
+        } else {
+            groups.push_back({0, 0});
+        }
+        for (const auto& g : groups) {
+            std::vector<BatchItem> sel;
+            for (const auto& it : items) {
+                const auto& v = p->eng[it.view]->v;
+                if (!rtdbs::batch_phase_split(ph) || (v.precision == g.first && v.dim == g.second))
+                    sel.push_back(it);
+            }
+            std::vector<int> prefix(sel.size() + 1, 0);
+            int max_c = 0;
+            for (size_t i = 0; i < sel.size(); ++i) {
+                prefix[i + 1] = prefix[i] + rtdbs::batch_blocks(ph, p->eng[sel[i].view]->v, sel[i].c);
+                max_c = std::max(max_c, sel[i].c);
+            }
+            const size_t items_off = put(sel.data(), sizeof(BatchItem) * sel.size());
+            const size_t prefix_off = put(prefix.data(), sizeof(int) * prefix.size());
+            plan.push_back({ph, g.first, g.second, items_off, prefix_off, (int)sel.size(), prefix.back(), max_c});
+        }
+    };
     std::vector<BatchItem> all_items;
     for (int j = 0; j < maxchunks; ++j) {
         std::vector<BatchItem> items;
@@ -725,26 +757,10 @@ int pool_build_shape(rtdbs_pool* p, const std::vector<int>& ids) {
             items.push_back(it);
         }
         if (j == 0) all_items = items;
-        const size_t items_off = put(items.data(), sizeof(BatchItem) * items.size());
-        for (int ph = 0; ph < rtdbs::kBatchChunkPhases; ++ph) {
-            std::vector<int> prefix(items.size() + 1, 0);
-            int max_c = 0;
-            for (size_t i = 0; i < items.size(); ++i) {
-                prefix[i + 1] = prefix[i] + rtdbs::batch_blocks(ph, p->eng[items[i].view]->v, items[i].c);
-                max_c = std::max(max_c, items[i].c);
-            }
-            const size_t prefix_off = put(prefix.data(), sizeof(int) * prefix.size());
-            plan.push_back({ph, items_off, prefix_off, (int)items.size(), prefix.back(), max_c});
-        }
+        for (int ph = 0; ph < rtdbs::kBatchChunkPhases; ++ph) add_launches(ph, items);
     }
-    const size_t all_off = put(all_items.data(), sizeof(BatchItem) * all_items.size());
-    for (int ph = rtdbs::kBatchUnion; ph <= rtdbs::kBatchLabel; ++ph) {
-        std::vector<int> prefix(all_items.size() + 1, 0);
-        for (size_t i = 0; i < all_items.size(); ++i)
-            prefix[i + 1] = prefix[i] + rtdbs::batch_blocks(ph, p->eng[all_items[i].view]->v, 0);
-        const size_t prefix_off = put(prefix.data(), sizeof(int) * prefix.size());
-        plan.push_back({ph, all_off, prefix_off, (int)all_items.size(), prefix.back(), 0});
-    }
+    for (auto& it : all_items) it.c = 0;  // cluster phases size by W only
+    for (int ph = rtdbs::kBatchUnion; ph <= rtdbs::kBatchLabel; ++ph) add_launches(ph, all_items);
     if (img.size() > p->tables_cap) {
         if (p->d_tables) cudaFree(p->d_tables);
         p->d_tables = nullptr;
@@ -767,7 +783,7 @@ int pool_enqueue_round(rtdbs_pool* p) {
         L.items = reinterpret_cast<const rtdbs::BatchItem*>(p->d_tables + l.items_off);
         L.prefix = reinterpret_cast<const int*>(p->d_tables + l.prefix_off);
         L.n = l.n;
-        CUDA_TRY(rtdbs::launch_batch(l.phase, L, l.blocks, l.max_c, p->stream));
+        CUDA_TRY(rtdbs::launch_batch(l.phase, l.prec, l.dim, L, l.blocks, l.max_c, p->stream));
     }
     return RTDBS_OK;
 }
@@ -1043,7 +1059,7 @@ int rtdbs_pool_slide_profiled(rtdbs_pool* p, int32_t n, const int32_t* ids, cons
         L.items = reinterpret_cast<const rtdbs::BatchItem*>(p->d_tables + l.items_off);
         L.prefix = reinterpret_cast<const int*>(p->d_tables + l.prefix_off);
         L.n = l.n;
-        cudaError_t ce = rtdbs::launch_batch(l.phase, L, l.blocks, l.max_c, p->stream);
+        cudaError_t ce = rtdbs::launch_batch(l.phase, l.prec, l.dim, L, l.blocks, l.max_c, p->stream);
         if (ce != cudaSuccess) rc = fail(RTDBS_ERR_CUDA, "launch failed: %s", cudaGetErrorString(ce));
         cudaEventRecord(ev[i + 1], p->stream);
     }

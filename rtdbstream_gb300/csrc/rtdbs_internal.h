@@ -184,7 +184,11 @@ struct BatchLaunch {
 // Blocks one item needs in a phase (same shapes as the single-stream launches).
 int batch_blocks(int phase, const View& v, int c);
 int batch_threads(int phase);
-cudaError_t launch_batch(int phase, const BatchLaunch& L, int total_blocks, int max_c, cudaStream_t s);
+// Phases launched once per (precision, dim) group of streams (the others
+// take every stream in one launch; prec and dim are then ignored).
+bool batch_phase_split(int phase);
+cudaError_t launch_batch(int phase, int prec, int dim, const BatchLaunch& L, int total_blocks, int max_c,
+                         cudaStream_t s);
 // Packs n device arrays (count[i] floats from src[i]) into dst at dst_off[i];
 // the three tables are device memory.
 cudaError_t launch_gather(const float* const* src, const long long* dst_off, const int* count, float* dst,

@@ -1302,19 +1302,6 @@ __global__ void k_counts_by_slot(View v, int* nn) {
 int g_num_sms = 0;
 // ------------------------------------------------------------- batched kernel
 
-#define RTDBS_BODY_DISPATCH(prec, dim, BODY, ...)                                 \
-    do {                                                                           \
-        if ((prec) == kPrecFp32) {                                                 \
-            if ((dim) == 1) BODY<kPrecFp32, 1>(__VA_ARGS__);                       \
-            else if ((dim) == 2) BODY<kPrecFp32, 2>(__VA_ARGS__);                  \
-            else BODY<kPrecFp32, 3>(__VA_ARGS__);                                  \
-        } else {                                                                   \
-            if ((dim) == 1) BODY<kPrecFp64, 1>(__VA_ARGS__);                       \
-            else if ((dim) == 2) BODY<kPrecFp64, 2>(__VA_ARGS__);                  \
-            else BODY<kPrecFp64, 3>(__VA_ARGS__);                                  \
-        }                                                                          \
-    } while (0)
-
 template <int PHASE>
 struct PhaseShape;
 template <> struct PhaseShape<kBatchIngest> { static constexpr int threads = 256, min_blocks = 1; };
@@ -1325,12 +1312,16 @@ template <> struct PhaseShape<kBatchMerge> { static constexpr int threads = kMer
 template <> struct PhaseShape<kBatchBuild> { static constexpr int threads = kBuildThreads, min_blocks = 1; };
 template <> struct PhaseShape<kBatchIncrement> { static constexpr int threads = 256, min_blocks = 8; };
 template <> struct PhaseShape<kBatchUnion> { static constexpr int threads = kClusterThreads, min_blocks = 8; };
-template <> struct PhaseShape<kBatchFlatten> { static constexpr int threads = 256, min_blocks = 1; };
+template <> struct PhaseShape<kBatchFlatten> { static constexpr int threads = 256, min_blocks = 6; };
 template <> struct PhaseShape<kBatchLabel> { static constexpr int threads = kClusterThreads, min_blocks = 6; };
 
 // One phase over many streams.  The block finds its item, copies that
 // stream's View into shared memory and runs the stream's kernel body.
-template <int PHASE>
+// Phases whose bodies depend on the precision mode and dimension are
+// instantiated per (MODE, DIM) and launched once per group of streams that
+// share them, so each instantiation holds one body (registers as in the
+// single-stream kernels); the other phases use MODE = DIM = 0.
+template <int PHASE, int MODE, int DIM>
 __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>::min_blocks)
     k_batch(BatchLaunch L) {
     __shared__ View sv;
@@ -1357,7 +1348,6 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
     }
     __syncthreads();
     const int bx = s_bx, nbx = s_nbx;
-    const int prec = sv.precision, dim = sv.dim;
     if constexpr (PHASE == kBatchIngest) {
         ingest_body(sv, it.j, it.c, 0, it.stg_off, it.input, bx);
     } else if constexpr (PHASE == kBatchSort) {
@@ -1370,7 +1360,7 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
         runmerge_body(sv, it.c, 0, bx % nruns, bx / nruns, words);
     } else if constexpr (PHASE == kBatchDecrement) {
         __shared__ StreamSmem sm;
-        RTDBS_BODY_DISPATCH(prec, dim, decr_body, sv, it.j, it.c, bx, sm);
+        decr_body<MODE, DIM>(sv, it.j, it.c, bx, sm);
     } else if constexpr (PHASE == kBatchMerge) {
         __shared__ MergeSmem sm;
         merge_body(sv, it.j, it.c, 0, bx, nbx, sm);
@@ -1379,19 +1369,19 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
         build_body(sv, bx, sm);
     } else if constexpr (PHASE == kBatchIncrement) {
         __shared__ StreamSmem sm;
-        RTDBS_BODY_DISPATCH(prec, dim, incr_body, sv, it.j, it.c, 0, bx, sm);
+        incr_body<MODE, DIM>(sv, it.j, it.c, 0, bx, sm);
     } else if constexpr (PHASE == kBatchUnion) {
         __shared__ ClusterSmem sm;
-        RTDBS_BODY_DISPATCH(prec, dim, union_body, sv, sm);
+        union_body<MODE, DIM>(sv, sm);
     } else if constexpr (PHASE == kBatchFlatten) {
         __shared__ StreamSmem sm;
-        RTDBS_BODY_DISPATCH(prec, dim, flatten_body, sv, bx, nbx, sm);
+        flatten_body<MODE, DIM>(sv, bx, nbx, sm);
     } else {
         __shared__ ClusterSmem sm;
         if (sv.list_cap >= 0)
             border_body(sv, 1, bx, nbx);
         else
-            RTDBS_BODY_DISPATCH(prec, dim, label_body, sv, 1, bx, sm);
+            label_body<MODE, DIM>(sv, 1, bx, sm);
     }
 }
 
@@ -1406,7 +1396,7 @@ void ensure_runmerge_smem() {
     if (g_runmerge_ready.load() & bit) return;
     const int bytes = (int)(sizeof(unsigned long long) * kChunkMax);
     if (cudaFuncSetAttribute(k_runmerge, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess &&
-        cudaFuncSetAttribute(k_batch<kBatchRunmerge>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) ==
+        cudaFuncSetAttribute(k_batch<kBatchRunmerge, 0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) ==
             cudaSuccess)
         g_runmerge_ready.fetch_or(bit);
 }
@@ -1538,23 +1528,42 @@ int batch_blocks(int phase, const View& v, int c) {
     }
 }
 
-cudaError_t launch_batch(int phase, const BatchLaunch& L, int total_blocks, int max_c, cudaStream_t s) {
+bool batch_phase_split(int phase) {
+    return phase == kBatchDecrement || phase == kBatchIncrement || phase == kBatchUnion ||
+           phase == kBatchFlatten || phase == kBatchLabel;
+}
+
+#define RTDBS_BATCH_MD(PH, GRID, BLOCK, STREAM)                                      \
+    do {                                                                           \
+        if (prec == kPrecFp32) {                                                   \
+            if (dim == 1) k_batch<PH, kPrecFp32, 1><<<GRID, BLOCK, 0, STREAM>>>(L);  \
+            else if (dim == 2) k_batch<PH, kPrecFp32, 2><<<GRID, BLOCK, 0, STREAM>>>(L); \
+            else k_batch<PH, kPrecFp32, 3><<<GRID, BLOCK, 0, STREAM>>>(L);           \
+        } else {                                                                   \
+            if (dim == 1) k_batch<PH, kPrecFp64, 1><<<GRID, BLOCK, 0, STREAM>>>(L);  \
+            else if (dim == 2) k_batch<PH, kPrecFp64, 2><<<GRID, BLOCK, 0, STREAM>>>(L); \
+            else k_batch<PH, kPrecFp64, 3><<<GRID, BLOCK, 0, STREAM>>>(L);           \
+        }                                                                          \
+    } while (0)
+
+cudaError_t launch_batch(int phase, int prec, int dim, const BatchLaunch& L, int total_blocks, int max_c,
+                         cudaStream_t s) {
     if (total_blocks <= 0 || L.n <= 0) return cudaSuccess;
     const int t = batch_threads(phase);
     switch (phase) {
-        case kBatchIngest: k_batch<kBatchIngest><<<total_blocks, t, 0, s>>>(L); break;
-        case kBatchSort: k_batch<kBatchSort><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchIngest: k_batch<kBatchIngest, 0, 0><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchSort: k_batch<kBatchSort, 0, 0><<<total_blocks, t, 0, s>>>(L); break;
         case kBatchRunmerge:
             ensure_runmerge_smem();
-            k_batch<kBatchRunmerge><<<total_blocks, t, sizeof(unsigned long long) * max_c, s>>>(L);
+            k_batch<kBatchRunmerge, 0, 0><<<total_blocks, t, sizeof(unsigned long long) * max_c, s>>>(L);
             break;
-        case kBatchDecrement: k_batch<kBatchDecrement><<<total_blocks, t, 0, s>>>(L); break;
-        case kBatchMerge: k_batch<kBatchMerge><<<total_blocks, t, 0, s>>>(L); break;
-        case kBatchBuild: k_batch<kBatchBuild><<<total_blocks, t, 0, s>>>(L); break;
-        case kBatchIncrement: k_batch<kBatchIncrement><<<total_blocks, t, 0, s>>>(L); break;
-        case kBatchUnion: k_batch<kBatchUnion><<<total_blocks, t, 0, s>>>(L); break;
-        case kBatchFlatten: k_batch<kBatchFlatten><<<total_blocks, t, 0, s>>>(L); break;
-        case kBatchLabel: k_batch<kBatchLabel><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchMerge: k_batch<kBatchMerge, 0, 0><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchBuild: k_batch<kBatchBuild, 0, 0><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchDecrement: RTDBS_BATCH_MD(kBatchDecrement, total_blocks, t, s); break;
+        case kBatchIncrement: RTDBS_BATCH_MD(kBatchIncrement, total_blocks, t, s); break;
+        case kBatchUnion: RTDBS_BATCH_MD(kBatchUnion, total_blocks, t, s); break;
+        case kBatchFlatten: RTDBS_BATCH_MD(kBatchFlatten, total_blocks, t, s); break;
+        case kBatchLabel: RTDBS_BATCH_MD(kBatchLabel, total_blocks, t, s); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
