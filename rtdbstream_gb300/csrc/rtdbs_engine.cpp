@@ -656,6 +656,12 @@ struct rtdbs_pool {
     size_t input_cap = 0;             // floats
     void* d_gather = nullptr;         // per-stream source pointers, offsets, counts
     size_t gather_cap = 0;
+    // side streams for the stream groups of a split phase, which run at the
+    // same time (fork/join through events; captured into the round's graph)
+    static constexpr int kSide = 5;
+    cudaStream_t side[kSide] = {};
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_join[kSide] = {};
     std::vector<int> shape_ids;       // stream set the tables / graph were built for
     cudaGraphExec_t graph = nullptr;
     // launch plan of the cached shape
@@ -776,14 +782,37 @@ int pool_build_shape(rtdbs_pool* p, const std::vector<int>& ids) {
     return RTDBS_OK;
 }
 
+cudaError_t pool_launch(rtdbs_pool* p, const rtdbs_pool::Launch& l, cudaStream_t s) {
+    rtdbs::BatchLaunch L;
+    L.views = p->d_views;
+    L.items = reinterpret_cast<const rtdbs::BatchItem*>(p->d_tables + l.items_off);
+    L.prefix = reinterpret_cast<const int*>(p->d_tables + l.prefix_off);
+    L.n = l.n;
+    return rtdbs::launch_batch(l.phase, l.prec, l.dim, L, l.blocks, l.max_c, s);
+}
+
+// One round.  The group launches of a split phase (consecutive plan entries
+// of one phase) are independent -- disjoint streams of the pool -- so they
+// run side by side: the first on the pool's stream, the others on side
+// streams forked from it and joined back before the next phase.
 int pool_enqueue_round(rtdbs_pool* p) {
-    for (const auto& l : p->plan) {
-        rtdbs::BatchLaunch L;
-        L.views = p->d_views;
-        L.items = reinterpret_cast<const rtdbs::BatchItem*>(p->d_tables + l.items_off);
-        L.prefix = reinterpret_cast<const int*>(p->d_tables + l.prefix_off);
-        L.n = l.n;
-        CUDA_TRY(rtdbs::launch_batch(l.phase, l.prec, l.dim, L, l.blocks, l.max_c, p->stream));
+    const size_t n = p->plan.size();
+    for (size_t i = 0; i < n;) {
+        size_t j = i + 1;
+        while (j < n && j - i <= (size_t)rtdbs_pool::kSide && p->plan[j].phase == p->plan[i].phase &&
+               rtdbs::batch_phase_split(p->plan[i].phase))
+            ++j;
+        if (j - i > 1) {
+            CUDA_TRY(cudaEventRecord(p->ev_fork, p->stream));
+            for (size_t g = 1; g < j - i; ++g) {
+                CUDA_TRY(cudaStreamWaitEvent(p->side[g - 1], p->ev_fork, 0));
+                CUDA_TRY(pool_launch(p, p->plan[i + g], p->side[g - 1]));
+                CUDA_TRY(cudaEventRecord(p->ev_join[g - 1], p->side[g - 1]));
+            }
+        }
+        CUDA_TRY(pool_launch(p, p->plan[i], p->stream));
+        for (size_t g = 1; g < j - i; ++g) CUDA_TRY(cudaStreamWaitEvent(p->stream, p->ev_join[g - 1], 0));
+        i = j;
     }
     return RTDBS_OK;
 }
@@ -833,6 +862,12 @@ int rtdbs_pool_create(const rtdbs_pool_params* pp, void* cuda_stream, rtdbs_pool
         rc = fail(RTDBS_ERR_OOM, "pool tables: allocation failed");
     if (rc == RTDBS_OK && cudaMemset(p->d_ctls, 0, sizeof(Ctl) * p->capacity) != cudaSuccess)
         rc = fail(RTDBS_ERR_CUDA, "cudaMemset failed");
+    if (rc == RTDBS_OK && cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming) != cudaSuccess)
+        rc = fail(RTDBS_ERR_CUDA, "cudaEventCreate failed");
+    for (int k = 0; k < rtdbs_pool::kSide && rc == RTDBS_OK; ++k)
+        if (cudaStreamCreateWithFlags(&p->side[k], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&p->ev_join[k], cudaEventDisableTiming) != cudaSuccess)
+            rc = fail(RTDBS_ERR_CUDA, "side stream set-up failed");
     if (rc != RTDBS_OK) {
         rtdbs_pool_destroy(p);
         return rc;
@@ -854,6 +889,11 @@ int rtdbs_pool_destroy(rtdbs_pool* p) {
     if (p->d_tables) cudaFree(p->d_tables);
     if (p->d_input) cudaFree(p->d_input);
     if (p->d_gather) cudaFree(p->d_gather);
+    for (int k = 0; k < rtdbs_pool::kSide; ++k) {
+        if (p->side[k]) cudaStreamDestroy(p->side[k]);
+        if (p->ev_join[k]) cudaEventDestroy(p->ev_join[k]);
+    }
+    if (p->ev_fork) cudaEventDestroy(p->ev_fork);
     if (p->own_stream && p->stream) cudaStreamDestroy(p->stream);
     delete p;
     return RTDBS_OK;
