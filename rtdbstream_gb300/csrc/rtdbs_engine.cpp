@@ -656,9 +656,8 @@ struct rtdbs_pool {
     size_t input_cap = 0;             // floats
     void* d_gather = nullptr;         // per-stream source pointers, offsets, counts
     size_t gather_cap = 0;
-    // side streams for the (precision, dim) groups of streams, whose launch
-    // chains run at the same time (fork/join through events; captured into
-    // the round's graph)
+    // side streams for the stream groups of a split phase, which run at the
+    // same time (fork/join through events; captured into the round's graph)
     static constexpr int kSide = 5;
     cudaStream_t side[kSide] = {};
     cudaEvent_t ev_fork = nullptr;
@@ -717,23 +716,26 @@ int pool_build_shape(rtdbs_pool* p, const std::vector<int>& ids) {
         return at;
     };
     std::vector<rtdbs_pool::Launch> plan;
-    // Phase ph over `items`: one launch per (precision, dim) group of
-    // streams, the groups in a fixed order (each group's launches form one
-    // chain, run beside the other groups' chains).
-    std::vector<std::pair<int, int>> groups;
-    for (int i = 0; i < n; ++i) {
-        const auto& v = p->eng[ids[i]]->v;
-        const std::pair<int, int> g(v.precision, v.dim);
-        if (std::find(groups.begin(), groups.end(), g) == groups.end()) groups.push_back(g);
-    }
+    // One launch of phase ph over `items`; split phases get one launch per
+    // (precision, dim) group present.
     auto add_launches = [&](int ph, const std::vector<BatchItem>& items) {
+        std::vector<std::pair<int, int>> groups;
+        if (rtdbs::batch_phase_split(ph)) {
+            for (const auto& it : items) {
+                const auto& v = p->eng[it.view]->v;
+                const std::pair<int, int> g(v.precision, v.dim);
+                if (std::find(groups.begin(), groups.end(), g) == groups.end()) groups.push_back(g);
+            }
+        } else {
+            groups.push_back({0, 0});
+        }
         for (const auto& g : groups) {
             std::vector<BatchItem> sel;
             for (const auto& it : items) {
                 const auto& v = p->eng[it.view]->v;
-                if (v.precision == g.first && v.dim == g.second) sel.push_back(it);
+                if (!rtdbs::batch_phase_split(ph) || (v.precision == g.first && v.dim == g.second))
+                    sel.push_back(it);
             }
-            if (sel.empty()) continue;
             std::vector<int> prefix(sel.size() + 1, 0);
             int max_c = 0;
             for (size_t i = 0; i < sel.size(); ++i) {
@@ -789,31 +791,28 @@ cudaError_t pool_launch(rtdbs_pool* p, const rtdbs_pool::Launch& l, cudaStream_t
     return rtdbs::launch_batch(l.phase, l.prec, l.dim, L, l.blocks, l.max_c, s);
 }
 
-// One round.  Each (precision, dim) group of streams is an independent
-// chain of launches (the groups hold disjoint streams of the pool), so the
-// chains run side by side: the first group's on the pool's stream, the
-// others on side streams forked from it at the start of the round and joined
-// back at its end.
+// One round.  The group launches of a split phase (consecutive plan entries
+// of one phase) are independent -- disjoint streams of the pool -- so they
+// run side by side: the first on the pool's stream, the others on side
+// streams forked from it and joined back before the next phase.
 int pool_enqueue_round(rtdbs_pool* p) {
-    std::vector<std::pair<int, int>> groups;
-    for (const auto& l : p->plan) {
-        const std::pair<int, int> g(l.prec, l.dim);
-        if (std::find(groups.begin(), groups.end(), g) == groups.end()) groups.push_back(g);
-    }
-    const int ng = (int)groups.size();
-    if (ng > 1 + rtdbs_pool::kSide) return fail(RTDBS_ERR_INVALID, "too many stream groups");
-    auto stream_of = [&](const rtdbs_pool::Launch& l) {
-        const int g = (int)(std::find(groups.begin(), groups.end(), std::make_pair(l.prec, l.dim)) - groups.begin());
-        return g == 0 ? p->stream : p->side[g - 1];
-    };
-    if (ng > 1) {
-        CUDA_TRY(cudaEventRecord(p->ev_fork, p->stream));
-        for (int g = 1; g < ng; ++g) CUDA_TRY(cudaStreamWaitEvent(p->side[g - 1], p->ev_fork, 0));
-    }
-    for (const auto& l : p->plan) CUDA_TRY(pool_launch(p, l, stream_of(l)));
-    for (int g = 1; g < ng; ++g) {
-        CUDA_TRY(cudaEventRecord(p->ev_join[g - 1], p->side[g - 1]));
-        CUDA_TRY(cudaStreamWaitEvent(p->stream, p->ev_join[g - 1], 0));
+    const size_t n = p->plan.size();
+    for (size_t i = 0; i < n;) {
+        size_t j = i + 1;
+        while (j < n && j - i <= (size_t)rtdbs_pool::kSide && p->plan[j].phase == p->plan[i].phase &&
+               rtdbs::batch_phase_split(p->plan[i].phase))
+            ++j;
+        if (j - i > 1) {
+            CUDA_TRY(cudaEventRecord(p->ev_fork, p->stream));
+            for (size_t g = 1; g < j - i; ++g) {
+                CUDA_TRY(cudaStreamWaitEvent(p->side[g - 1], p->ev_fork, 0));
+                CUDA_TRY(pool_launch(p, p->plan[i + g], p->side[g - 1]));
+                CUDA_TRY(cudaEventRecord(p->ev_join[g - 1], p->side[g - 1]));
+            }
+        }
+        CUDA_TRY(pool_launch(p, p->plan[i], p->stream));
+        for (size_t g = 1; g < j - i; ++g) CUDA_TRY(cudaStreamWaitEvent(p->stream, p->ev_join[g - 1], 0));
+        i = j;
     }
     return RTDBS_OK;
 }
