@@ -204,43 +204,62 @@ struct Stencil {
     static constexpr int kRows = kAllRows - kFirst;
 };
 
-// Row ranges of the stencil around `key`.  On return lane r < kRows holds
-// row r as [rs, re) (empty rows: rs == re).
-template <int DIM, bool HALF>
+// Row ranges of the stencil around `key`, computed by a group of G lanes
+// (the whole warp, or each 16-lane half for its own key; `lane` counts within
+// the group; a lane looks up one or two cells).  On return group lane
+// r < kRows holds row r as [rs, re) (empty rows: rs == re).
+template <int DIM, bool HALF, int G = 32>
 __device__ __forceinline__ void row_ranges(const View& v, const ulonglong2* T, unsigned gen,
                                            unsigned long long key, int lane, int& rs, int& re) {
     using St = Stencil<DIM, HALF>;
+    constexpr int kSlots = 3 * St::kRows;            // cell slots, kept row by kept row
+    constexpr int kPer = (kSlots + G - 1) / G;       // cells per lane
+    static_assert(kPer <= 2, "stencil too large for the lane group");
     const long long c2 = (long long)(key & ((1ull << v.shift[1]) - 1ull));
     const long long c1 = (long long)((key >> v.shift[1]) & ((1ull << (v.shift[0] - v.shift[1])) - 1ull));
     const long long c0 = (long long)(key >> v.shift[0]);
-    int2 rg = make_int2(0, 0);
-    const int row = St::kFirst + lane / 3, d_last = lane % 3 - 1;  // lane = 3 * kept row + cell
-    const bool skip = HALF && lane < 3 && d_last < 0;             // centre row, cell -1
-    if (lane < 3 * St::kRows && !skip) {
-        long long q0 = c0, q1 = c1, q2 = c2;
-        if (DIM == 1) {
-            q0 += d_last;
-        } else if (DIM == 2) {
-            q0 += row - 1;
-            q1 += d_last;
-        } else {
-            q0 += row / 3 - 1;
-            q1 += row % 3 - 1;
-            q2 += d_last;
-        }
-        const bool ok = q0 >= 0 && q0 < v.ext[0] && q1 >= 0 && q1 < v.ext[1] && q2 >= 0 && q2 < v.ext[2];
-        if (ok) {
-            const unsigned long long nk = ((unsigned long long)q0 << v.shift[0]) |
-                                          ((unsigned long long)q1 << v.shift[1]) | (unsigned long long)q2;
-            rg = table_find(T, v.pmask, v.pbits, tag_of(nk, gen));
+    int2 rg[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+        rg[k] = make_int2(0, 0);
+        const int cs = lane + k * G;                                  // = 3 * kept row + cell
+        const int row = St::kFirst + cs / 3, d_last = cs % 3 - 1;
+        const bool skip = HALF && cs < 3 && d_last < 0;              // centre row, cell -1
+        if (cs < kSlots && !skip) {
+            long long q0 = c0, q1 = c1, q2 = c2;
+            if (DIM == 1) {
+                q0 += d_last;
+            } else if (DIM == 2) {
+                q0 += row - 1;
+                q1 += d_last;
+            } else {
+                q0 += row / 3 - 1;
+                q1 += row % 3 - 1;
+                q2 += d_last;
+            }
+            const bool ok = q0 >= 0 && q0 < v.ext[0] && q1 >= 0 && q1 < v.ext[1] && q2 >= 0 && q2 < v.ext[2];
+            if (ok) {
+                const unsigned long long nk = ((unsigned long long)q0 << v.shift[0]) |
+                                              ((unsigned long long)q1 << v.shift[1]) | (unsigned long long)q2;
+                rg[k] = table_find(T, v.pmask, v.pbits, tag_of(nk, gen));
+            }
         }
     }
     int s = INT_MAX, e = INT_MIN;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const int src = min(3 * lane + k, 31);
-        const int a = __shfl_sync(kFull, rg.x, src);
-        const int b = __shfl_sync(kFull, rg.y, src);
+        const int cs = min(3 * lane + k, kSlots - 1);   // slot of row `lane`'s cell k
+        const int src = cs % G, which = cs / G;
+        int a = __shfl_sync(kFull, rg[0].x, src, G);
+        int b = __shfl_sync(kFull, rg[0].y, src, G);
+        if (kPer > 1) {
+            const int a1 = __shfl_sync(kFull, rg[kPer - 1].x, src, G);
+            const int b1 = __shfl_sync(kFull, rg[kPer - 1].y, src, G);
+            if (which) {
+                a = a1;
+                b = b1;
+            }
+        }
         if (b > a) {
             s = min(s, a);
             e = max(e, b);
@@ -251,11 +270,12 @@ __device__ __forceinline__ void row_ranges(const View& v, const ulonglong2* T, u
     re = e;
 }
 
-// The warp's row ranges (lanes 0..ROWS-1), clipped below at `lo`, laid end
-// to end: candidate idx in [0, total) lives at sorted position
+// The group's row ranges (group lanes 0..ROWS-1), clipped below at `lo`,
+// laid end to end: candidate idx in [0, total) lives at sorted position
 // start[r] + idx - pre[r] for the row r with pre[r] <= idx < pre[r+1].
-// Concatenating the rows keeps the 32-lane candidate chunks full.
-template <int ROWS>
+// Concatenating the rows keeps the candidate chunks full.  Called by the
+// whole warp; G-lane groups work independently.
+template <int ROWS, int G = 32>
 __device__ __forceinline__ int candidate_stream(int rs, int re, int lo, int lane, int* sstart,
                                                 int* spre) {
     const int a = max(rs, lo);
@@ -263,10 +283,10 @@ __device__ __forceinline__ int candidate_stream(int rs, int re, int lo, int lane
     int incl = len;
 #pragma unroll
     for (int o = 1; o < 16; o <<= 1) {
-        const int t = __shfl_up_sync(kFull, incl, o);
+        const int t = __shfl_up_sync(kFull, incl, o, G);
         if (lane >= o) incl += t;
     }
-    const int total = __shfl_sync(kFull, incl, ROWS - 1);
+    const int total = __shfl_sync(kFull, incl, ROWS - 1, G);
     __syncwarp();
     if (lane < ROWS) {
         sstart[lane] = a;
@@ -366,25 +386,35 @@ __device__ __forceinline__ void list_remove(const View& v, int q, int p) {
     atomicOr(&v.ctl->err, kErrList);
 }
 
-// Warp-wide: adds the lanes' neighbour slots (nb) to the warp's buffer in
-// lane order; returns the new number found (entries past cap are dropped,
-// the list is then not kept anyway).
+// Called by the whole warp; each group of G lanes (gl = lane within the
+// group) adds its lanes' neighbour slots (nb) to its own buffer in lane
+// order; returns the group's new number found (entries past cap are
+// dropped, the list is then not kept anyway).
+template <int G = 32>
 __device__ __forceinline__ int list_collect(bool nb, int qs, int nfound, int cap, int* buf, int lane) {
-    const unsigned m = __ballot_sync(kFull, nb);
-    const int at = nfound + __popc(m & lanemask_lt(lane));
+    const unsigned all = __ballot_sync(kFull, nb);
+    const int gl = lane & (G - 1);
+    const unsigned m = G == 32 ? all : (all >> (lane - gl)) & ((1u << G) - 1u);
+    const int at = nfound + __popc(m & lanemask_lt(gl));
     if (nb && at < cap) buf[at] = qs;
     return nfound + __popc(m);
 }
 
-// Warp-wide: writes slot a's list from the buffer (kept iff a is not core);
-// the row's padding past list_cap stays -1.
-__device__ __forceinline__ void list_store(const View& v, int a, int nfound, const int* buf, int lane) {
+// Called by the whole warp; a group with a point (`has`) writes slot a's
+// list from its buffer (kept iff a is not core); the row's padding past
+// list_cap stays -1.
+template <int G = 32>
+__device__ __forceinline__ void list_store(const View& v, int a, int nfound, const int* buf, int lane,
+                                           bool has = true) {
     __syncwarp();
-    const bool keep = nfound + 1 < v.min_pts;
-    int* L = v.nlist + (size_t)a * v.list_stride;
-    if (keep)
-        for (int k = lane; k < v.list_stride; k += 32) L[k] = k < nfound ? buf[k] : -1;
-    if (lane == 0) v.ntrack[a] = keep ? 1 : 0;
+    const int gl = lane & (G - 1);
+    if (has) {
+        const bool keep = nfound + 1 < v.min_pts;
+        int* L = v.nlist + (size_t)a * v.list_stride;
+        if (keep)
+            for (int k = gl; k < v.list_stride; k += G) L[k] = k < nfound ? buf[k] : -1;
+        if (gl == 0) v.ntrack[a] = keep ? 1 : 0;
+    }
     __syncwarp();
 }
 
@@ -551,38 +581,50 @@ __global__ void __launch_bounds__(kSortRun) k_runmerge(View v, int c, int init) 
 }
 
 // -1 on the count of every surviving neighbour of each expired point (old grid).
+// Points a count pass gives each warp: 1 (32 lanes each) or 2 (one per
+// 16-lane half), so two queries' dependent loads overlap.
+constexpr int kQueryLanes = 16;
+constexpr int kQueriesPerWarp = 32 / kQueryLanes;
+
 struct StreamSmem {
     int rstart[8][9], rpre[8][10];
+    int grstart[8][2][9], grpre[8][2][10];  // per 16-lane group (count passes)
     int nbuf[8][kListCap];
+    int gnbuf[8][2][kListCap];
     int queue[256];  // k_flatten: positions whose lists are rebuilt, in the block's tile
     int nq;
 };
 
 template <int MODE, int DIM>
 __device__ __forceinline__ void decr_body(const View& v, int j, int c, int bx, StreamSmem& sm) {
-    int(&rstart)[8][9] = sm.rstart;
-    int(&rpre)[8][10] = sm.rpre;
+    constexpr int G = kQueryLanes;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int grp = lane / G, gl = lane % G;
     const int gw = (bx * blockDim.x + threadIdx.x) >> 5;
-    if (gw >= c) return;
+    if (gw * kQueriesPerWarp >= c) return;
+    const int qi = gw * kQueriesPerWarp + grp;
+    const bool has = qi < c;
+    int* rstart = sm.grstart[wib][grp];
+    int* rpre = sm.grpre[wib][grp];
     const long long b = v.ctl->b;
     const int old = (int)((b - 1) & 1);
     const unsigned gen = gen_of_build(b - 1);
     const int el = chunk_base_slot(v, j, 0);
-    const unsigned long long word = v.xword[gw];
+    const unsigned long long word = has ? v.xword[qi] : 0ull;
     const unsigned long long key = word >> kOffBits;
-    const float4 xp = v.xpt[word & ((1u << kOffBits) - 1)];
+    const float4 xp = has ? v.xpt[word & ((1u << kOffBits) - 1)] : make_float4(0.f, 0.f, 0.f, 0.f);
     int rs, re;
-    row_ranges<DIM, false>(v, v.table[old], gen, key, lane, rs, re);
-    const int total = candidate_stream<Stencil<DIM, false>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
+    row_ranges<DIM, false, G>(v, v.table[old], gen, key, gl, rs, re);
+    int total = candidate_stream<Stencil<DIM, false>::kRows, G>(rs, re, 0, gl, rstart, rpre);
+    if (!has) total = 0;
     const float4* spt = v.spt[old];
     int* scnt = v.scnt[old];
     const bool lists = v.list_cap >= 0;
     const int xs = slot_of(xp);
     Tally tally;
     int r = 0;
-    for (int idx = lane; idx < total; idx += 32) {
-        const int pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
+    for (int idx = gl; idx < total; idx += G) {
+        const int pos = stream_pos(idx, r, rstart, rpre);
         const float4 q = spt[pos];
         const int cnt = scnt[pos];  // counts only fall here: >= MinPts means no list kept
         const int qs = slot_of(q);
@@ -901,34 +943,42 @@ __global__ void __launch_bounds__(kBuildThreads) k_build(View v) {
 // Full count of each new point and +1 on every older neighbour (new grid).
 template <int MODE, int DIM>
 __device__ __forceinline__ void incr_body(const View& v, int j, int c, int init, int bx, StreamSmem& sm) {
-    int(&rstart)[8][9] = sm.rstart;
-    int(&rpre)[8][10] = sm.rpre;
+    constexpr int G = kQueryLanes;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int grp = lane / G, gl = lane % G;
     const int gw = (bx * blockDim.x + threadIdx.x) >> 5;
-    if (gw >= c) return;
+    if (gw * kQueriesPerWarp >= c) return;
+    const int qi = gw * kQueriesPerWarp + grp;
+    const bool has = qi < c;
+    int* rstart = sm.grstart[wib][grp];
+    int* rpre = sm.grpre[wib][grp];
     const long long b = v.ctl->b;
     const int cur = (int)(b & 1);
     const unsigned gen = gen_of_build(b);
     const int el = chunk_base_slot(v, j, init);
-    const unsigned long long word = v.nword[gw];
+    const unsigned long long word = has ? v.nword[qi] : 0ull;
     const unsigned long long key = word >> kOffBits;
     const int aslot = el + (int)(word & ((1u << kOffBits) - 1));
-    const float4 ap = v.ring[aslot];
+    const float4 ap = has ? v.ring[aslot] : make_float4(0.f, 0.f, 0.f, 0.f);
     int rs, re;
-    row_ranges<DIM, false>(v, v.table[cur], gen, key, lane, rs, re);
-    const int total = candidate_stream<Stencil<DIM, false>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
+    row_ranges<DIM, false, G>(v, v.table[cur], gen, key, gl, rs, re);
+    int total = candidate_stream<Stencil<DIM, false>::kRows, G>(rs, re, 0, gl, rstart, rpre);
+    if (!has) total = 0;
+    int tmax = total;
+#pragma unroll
+    for (int o = G; o < 32; o <<= 1) tmax = max(tmax, __shfl_xor_sync(kFull, tmax, o));
     const float4* spt = v.spt[cur];
     int* scnt = v.scnt[cur];
     const bool lists = v.list_cap >= 0;
-    int* nbuf = sm.nbuf[wib];
+    int* nbuf = sm.gnbuf[wib][grp];
     Tally tally;
     int count = 0, mypos = -1, r = 0, nfound = 0;
-    for (int base = 0; base < total; base += 32) {
-        const int idx = base + lane;
+    for (int base = 0; base < tmax; base += G) {
+        const int idx = base + gl;
         bool nb = false;
         int qs = -1;
         if (idx < total) {
-            const int pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
+            const int pos = stream_pos(idx, r, rstart, rpre);
             const float4 q = spt[pos];
             const int cnt = scnt[pos];  // counts only rise here: >= MinPts means no list kept
             qs = slot_of(q);
@@ -944,14 +994,16 @@ __device__ __forceinline__ void incr_body(const View& v, int j, int c, int init,
                 }
             }
         }
-        if (lists) nfound = list_collect(nb, qs, nfound, v.list_cap, nbuf, lane);
+        if (lists) nfound = list_collect<G>(nb, qs, nfound, v.list_cap, nbuf, lane);
     }
-    if (lists) list_store(v, aslot, nfound, nbuf, lane);
+    if (lists) list_store<G>(v, aslot, nfound, nbuf, lane, has);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) count += __shfl_xor_sync(kFull, count, o);
-    mypos = (int)__reduce_max_sync(kFull, (unsigned)(mypos + 1)) - 1;
+    for (int o = G / 2; o > 0; o >>= 1) {
+        count += __shfl_xor_sync(kFull, count, o);
+        mypos = max(mypos, __shfl_xor_sync(kFull, mypos, o));
+    }
     int err = 0;
-    if (lane == 0) {
+    if (gl == 0 && has) {
         if (mypos >= 0)
             scnt[mypos] = count;
         else
@@ -1428,7 +1480,7 @@ cudaError_t configure_kernels() {
 
 cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, int init,
                          int stg_off, int advance, cudaStream_t s) {
-    const int warp_blocks = (c * 32 + 255) / 256;
+    const int warp_blocks = (c * kQueryLanes + 255) / 256;  // count passes: kQueryLanes per point
     switch (phase) {
         case kPhaseIngest:
             k_ingest<<<(c + 255) / 256, 256, 0, s>>>(v, j, c, init, stg_off);
@@ -1516,7 +1568,7 @@ int batch_blocks(int phase, const View& v, int c) {
         case kBatchSort:
         case kBatchRunmerge: return 2 * runs;
         case kBatchDecrement:
-        case kBatchIncrement: return (c * 32 + 255) / 256;
+        case kBatchIncrement: return (c * kQueryLanes + 255) / 256;
         case kBatchMerge: return (v.W + kMergeTile - 1) / kMergeTile;
         case kBatchBuild: return (v.W + kBuildThreads - 1) / kBuildThreads;
         case kBatchUnion: return max(1, min(1024, (v.W + 1023) / 1024));  // persistent, queue-fed
