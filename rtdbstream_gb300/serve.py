@@ -12,6 +12,7 @@ its memory.  Latency of a request = completion of its round - its arrival.
 from __future__ import annotations
 
 import collections
+import gc
 import time
 from dataclasses import dataclass, field
 from typing import List, Optional
@@ -72,8 +73,6 @@ class SlideServer:
         """Serve requests arriving at `arrivals` (seconds from the start,
         sorted) for stream indices `targets`; returns latency and throughput.
         The pool's CUDA stream must be torch's current stream."""
-        import torch
-
         base = [s.slide_data.data_ptr() for s in self.streams]
         row = [s.slide_data.shape[1] * s.slide_data.element_size() for s in self.streams]
         krow = [s.slide_data.shape[0] for s in self.streams]
@@ -82,6 +81,19 @@ class SlideServer:
         n = len(arrivals)
         nxt = 0
         active = set()                  # streams with pending requests
+        # no collector pauses inside the request loop (they would show as
+        # latency spikes); collect once the run is over
+        gc_was_on = gc.isenabled()
+        gc.disable()
+        try:
+            return self._loop(arrivals, targets, base, row, krow, lat, slid, n, nxt, active)
+        finally:
+            if gc_was_on:
+                gc.enable()
+
+    def _loop(self, arrivals, targets, base, row, krow, lat, slid, n, nxt, active) -> dict:
+        import torch
+
         t0 = time.perf_counter()
         while True:
             now = time.perf_counter() - t0
