@@ -194,7 +194,7 @@ size_t plan_layout(rtdbs_engine* e, std::vector<Part>& parts) {
     v.list_stride = v.list_cap > 0 ? (v.list_cap + 3) / 4 * 4 : 0;
     const size_t list_ints = (size_t)W * v.list_stride;
     const size_t track_ints = v.list_cap >= 0 ? (size_t)W : 0;
-    v.nlist = v.ntrack = v.rslot = nullptr;
+    v.nlist = v.ntrack = v.rslot = v.damaged = nullptr;
     parts = {
         {(void**)&v.ring, sizeof(float4) * W},
         {(void**)&v.kslot, sizeof(unsigned long long) * W},
@@ -214,6 +214,7 @@ size_t plan_layout(rtdbs_engine* e, std::vector<Part>& parts) {
         {(void**)&v.nlist, sizeof(int) * list_ints},
         {(void**)&v.ntrack, sizeof(int) * track_ints},
         {(void**)&v.rslot, sizeof(int) * track_ints},
+        {(void**)&v.damaged, sizeof(int) * track_ints},
         {(void**)&v.nsort, sizeof(unsigned long long) * C},
         {(void**)&v.xsort, sizeof(unsigned long long) * C},
         {(void**)&v.nword, sizeof(unsigned long long) * C},
@@ -551,7 +552,9 @@ int rtdbs_get_stats(rtdbs_engine* e, rtdbs_stats* s) {
     s->device_bytes = (int64_t)e->dev_bytes;
     const int nchunks = (e->p.stride + e->chunk - 1) / e->chunk;
     s->chunks_per_slide = nchunks;
-    s->launches_per_slide = nchunks * (rtdbs::kChunkPhases + 1) + 3;  // sort phase = 2 kernels
+    // sort phase = 2 kernels; with neighbour lists the union phase adds the
+    // two forest-reuse passes
+    s->launches_per_slide = nchunks * (rtdbs::kChunkPhases + 1) + 3 + (e->v.list_cap >= 0 ? 2 : 0);
     return RTDBS_OK;
 }
 
@@ -766,7 +769,7 @@ int pool_build_shape(rtdbs_pool* p, const std::vector<int>& ids) {
         for (int ph = 0; ph < rtdbs::kBatchChunkPhases; ++ph) add_launches(ph, items);
     }
     for (auto& it : all_items) it.c = 0;  // cluster phases size by W only
-    for (int ph = rtdbs::kBatchUnion; ph <= rtdbs::kBatchLabel; ++ph) add_launches(ph, all_items);
+    for (int ph = rtdbs::kBatchDamage; ph <= rtdbs::kBatchLabel; ++ph) add_launches(ph, all_items);
     if (img.size() > p->tables_cap) {
         if (p->d_tables) cudaFree(p->d_tables);
         p->d_tables = nullptr;
@@ -1106,7 +1109,8 @@ int rtdbs_pool_slide_profiled(rtdbs_pool* p, int32_t n, const int32_t* ids, cons
     if (rc == RTDBS_OK) rc = rtdbs_pool_sync(p);
     if (rc == RTDBS_OK) {
         // batch phases -> the engine's phase slots (sort + run merge are one)
-        static const int slot[rtdbs::kNumBatchPhases] = {0, 1, 1, 2, 3, 4, 5, 6, 7, 8};
+        // (the forest-reuse passes belong to the union phase, as in the single-stream launch)
+        static const int slot[rtdbs::kNumBatchPhases] = {0, 1, 1, 2, 3, 4, 5, 6, 6, 6, 7, 8};
         float ph[9] = {0};
         for (size_t i = 0; i < p->plan.size(); ++i) {
             float ms = 0.f;

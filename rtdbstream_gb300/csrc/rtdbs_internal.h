@@ -21,6 +21,7 @@
 //                         (cap = MinPts - 2 entries, rows padded to a multiple
 //                         of 4 for 16-byte loads; -1 = empty entry)
 //   rslot  i32[W]         per slot after the flatten: root (core) or -1
+//   damaged i32[W]        per previous root: the component lost a core this slide
 //   ntrack i32[W]         1: the slot's list is exact; 0: not kept (core, or
 //                         rebuilt at the end of the slide)
 //   chunk scratch: sort words, expired points.
@@ -62,7 +63,8 @@ struct Ctl {
     int nitems;                // work items of the current grid
     int ncells;                // cells of the current grid
     int err;                   // kErr* bits
-    int pad0;
+    int prev_ok;               // label/cid hold the clustering of the window before
+                               // this slide's changes (the forest can be reused)
     int union_next;            // next work item handed out by k_union
     int label_next;            // next work item handed out by k_label
     unsigned long long band_rechecks;
@@ -110,6 +112,8 @@ struct View {
     int* cid;
     int* nlist;                  // [W][list_stride] neighbours of non-core points
     int* rslot;                  // per slot: root of a core, -1 otherwise
+    int* damaged;                // per old root slot: its component lost a core this
+                                 // slide (0 outside the union phase)
     int* ntrack;                 // per slot: 1 list exact, 0 not kept
     unsigned long long* nsort;   // chunk sort words in (key << 14 | offset)
     unsigned long long* xsort;
@@ -159,6 +163,8 @@ enum BatchPhase : int {
     kBatchMerge,
     kBatchBuild,
     kBatchIncrement,
+    kBatchDamage,
+    kBatchReuse,
     kBatchUnion,
     kBatchFlatten,
     kBatchLabel,

@@ -1018,6 +1018,67 @@ __global__ void __launch_bounds__(256) k_incr(View v, int j, int c, int init) {
     incr_body<MODE, DIM>(v, j, c, init, blockIdx.x, sm);
 }
 
+// ------------------------------------------------------ forest reuse
+// A component of the previous clustering that lost no core this slide (no
+// core expired, no core fell below MinPts) is still connected: all its
+// cores and the edges between them remain.  Its cores start the union as
+// one set under the old root (still its minimum slot), with that root as
+// their hint, so pairs inside it are skipped by hint equality; every other
+// core starts as a singleton.  The union still visits every core pair, so
+// merges through new cores and splits of damaged components come out exactly
+// as in a union from scratch.  Used with neighbour lists, where k_border
+// leaves the previous labels and ids by slot and resets the forest.
+
+// The slide's new slots: [base, base + S).
+__device__ __forceinline__ bool slot_is_new(const View& v, int s) {
+    const int base = (int)(v.ctl->slide % v.units) * v.S;
+    return s >= base && s < base + v.S;
+}
+
+// Marks the old root of every core lost this slide: expired cores (slots of
+// the new points, read before the border pass overwrites them) and cores
+// now below MinPts.
+__device__ __forceinline__ void damage_body(const View& v, int bx, int nbx) {
+    if (!v.ctl->prev_ok) return;
+    const int cur = (int)(v.ctl->b & 1);
+    const int n = v.ctl->nocc[cur];
+    const int* scnt = v.scnt[cur];
+    const int* sw = reinterpret_cast<const int*>(v.spt[cur]) + 3;  // .w = slot
+    const int base = (int)(v.ctl->slide % v.units) * v.S;
+    for (int i = bx * blockDim.x + threadIdx.x; i < n + v.S; i += nbx * blockDim.x) {
+        int s;
+        if (i < n) {
+            if (scnt[i] >= v.min_pts) continue;
+            s = sw[4 * (size_t)i];
+            if (slot_is_new(v, s)) continue;
+        } else {
+            s = base + (i - n);  // an expired point's slot
+        }
+        if (v.label[s] == 0) v.damaged[v.cid[s]] = 1;
+    }
+}
+
+// Cores of intact components join their old root (parent and hint).
+__device__ __forceinline__ void reuse_body(const View& v, int bx, int nbx) {
+    if (!v.ctl->prev_ok) return;
+    const int cur = (int)(v.ctl->b & 1);
+    const int n = v.ctl->nocc[cur];
+    const int* scnt = v.scnt[cur];
+    const int* sw = reinterpret_cast<const int*>(v.spt[cur]) + 3;
+    for (int i = bx * blockDim.x + threadIdx.x; i < n; i += nbx * blockDim.x) {
+        if (scnt[i] < v.min_pts) continue;
+        const int s = sw[4 * (size_t)i];
+        if (v.label[s] != 0 || slot_is_new(v, s)) continue;
+        const int r = v.cid[s];
+        if (v.damaged[r]) continue;
+        v.parent[s] = r;
+        v.sroot[i] = r;
+    }
+}
+
+__global__ void k_damage(View v) { damage_body(v, blockIdx.x, gridDim.x); }
+__global__ void k_reuse(View v) { reuse_body(v, blockIdx.x, gridDim.x); }
+
 // Union of every core-core neighbour pair, each unordered pair once (the
 // candidate's sorted position is above the home point's).  A candidate's
 // root is found once per candidate chunk and compared with cached roots of
@@ -1335,9 +1396,11 @@ __device__ __forceinline__ void border_body(const View& v, int advance, int bx, 
         v.label[s] = lab;
         v.cid[s] = id;
         v.parent[s] = s;
+        v.damaged[s] = 0;
     }
     if (bx == 0 && threadIdx.x == 0) {
         v.ctl->union_next = 0;                // the next clustering's queue; not read here
+        v.ctl->prev_ok = 1;                   // the forest of this clustering can be reused
         if (advance) v.ctl->slide += 1;       // no reader here
     }
 }
@@ -1363,6 +1426,8 @@ template <> struct PhaseShape<kBatchDecrement> { static constexpr int threads = 
 template <> struct PhaseShape<kBatchMerge> { static constexpr int threads = kMergeThreads, min_blocks = 1; };
 template <> struct PhaseShape<kBatchBuild> { static constexpr int threads = kBuildThreads, min_blocks = 1; };
 template <> struct PhaseShape<kBatchIncrement> { static constexpr int threads = 256, min_blocks = 8; };
+template <> struct PhaseShape<kBatchDamage> { static constexpr int threads = 256, min_blocks = 1; };
+template <> struct PhaseShape<kBatchReuse> { static constexpr int threads = 256, min_blocks = 1; };
 template <> struct PhaseShape<kBatchUnion> { static constexpr int threads = kClusterThreads, min_blocks = 8; };
 template <> struct PhaseShape<kBatchFlatten> { static constexpr int threads = 256, min_blocks = 6; };
 template <> struct PhaseShape<kBatchLabel> { static constexpr int threads = kClusterThreads, min_blocks = 6; };
@@ -1422,6 +1487,10 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
     } else if constexpr (PHASE == kBatchIncrement) {
         __shared__ StreamSmem sm;
         incr_body<MODE, DIM>(sv, it.j, it.c, 0, bx, sm);
+    } else if constexpr (PHASE == kBatchDamage) {
+        if (sv.list_cap >= 0) damage_body(sv, bx, nbx);
+    } else if constexpr (PHASE == kBatchReuse) {
+        if (sv.list_cap >= 0) reuse_body(sv, bx, nbx);
     } else if constexpr (PHASE == kBatchUnion) {
         __shared__ ClusterSmem sm;
         union_body<MODE, DIM>(sv, sm);
@@ -1511,6 +1580,12 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
             }
             [[fallthrough]];
         case kPhaseUnion: {
+            if (v.list_cap >= 0) {
+                const int sms0 = g_num_sms > 0 ? g_num_sms : 152;
+                const int rb = max(1, min(sms0 * 8, (v.W + 255) / 256));
+                k_damage<<<rb, 256, 0, s>>>(v);
+                k_reuse<<<rb, 256, 0, s>>>(v);
+            }
             const int sms = g_num_sms > 0 ? g_num_sms : 152;
             const int per_block = kClusterThreads / 32;
             const int need = (v.max_items + per_block - 1) / per_block;  // one warp per item at most
@@ -1571,6 +1646,8 @@ int batch_blocks(int phase, const View& v, int c) {
         case kBatchIncrement: return (c * kQueryLanes + 255) / 256;
         case kBatchMerge: return (v.W + kMergeTile - 1) / kMergeTile;
         case kBatchBuild: return (v.W + kBuildThreads - 1) / kBuildThreads;
+        case kBatchDamage:
+        case kBatchReuse: return v.list_cap >= 0 ? max(1, min(1024, (v.W + 2047) / 2048)) : 0;
         case kBatchUnion: return max(1, min(1024, (v.W + 1023) / 1024));  // persistent, queue-fed
         case kBatchLabel:
             if (v.list_cap >= 0) return max(1, min(1024, (v.W + 1023) / 1024));  // k_border
@@ -1613,6 +1690,8 @@ cudaError_t launch_batch(int phase, int prec, int dim, const BatchLaunch& L, int
         case kBatchBuild: k_batch<kBatchBuild, 0, 0><<<total_blocks, t, 0, s>>>(L); break;
         case kBatchDecrement: RTDBS_BATCH_MD(kBatchDecrement, total_blocks, t, s); break;
         case kBatchIncrement: RTDBS_BATCH_MD(kBatchIncrement, total_blocks, t, s); break;
+        case kBatchDamage: k_batch<kBatchDamage, 0, 0><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchReuse: k_batch<kBatchReuse, 0, 0><<<total_blocks, t, 0, s>>>(L); break;
         case kBatchUnion: RTDBS_BATCH_MD(kBatchUnion, total_blocks, t, s); break;
         case kBatchFlatten: RTDBS_BATCH_MD(kBatchFlatten, total_blocks, t, s); break;
         case kBatchLabel: RTDBS_BATCH_MD(kBatchLabel, total_blocks, t, s); break;
