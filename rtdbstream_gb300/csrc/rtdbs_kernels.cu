@@ -1140,8 +1140,14 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
         const unsigned hmask = __ballot_sync(kFull, hcore);
         if (!hmask) continue;
         __syncwarp();
-        if (hcore) rh[lane] = hint[start + lane];
+        const int hh = hcore ? hint[start + lane] : 0;
+        if (hcore) rh[lane] = hh;
         home_pt[wib][lane] = h;
+        // All home cores under one hint r0 (common once the previous forest is
+        // reused): a candidate chunk whose cores all carry r0 is one set with
+        // them and is skipped without the per-home loop.
+        const int r0 = __shfl_sync(kFull, hh, __ffs(hmask) - 1);
+        const bool uni = __all_sync(kFull, !hcore || hh == r0);
         const int hmin = start + __ffs(hmask) - 1;
         int rs, re;
         row_ranges<DIM, true>(v, T, gen, skey[start], lane, rs, re);
@@ -1159,7 +1165,7 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
                 qh = hint[pos];
                 qc = qn >= v.min_pts;
             }
-            if (!__any_sync(kFull, qc)) continue;
+            if (!__any_sync(kFull, qc && !(uni && qh == r0))) continue;
             // Pairs whose hints already agree are in one set: no test, no link.
             unsigned adj = 0;
             unsigned mm = hmask;
