@@ -69,7 +69,9 @@ struct Ctl {
     int label_next;            // next work item handed out by k_label
     unsigned long long band_rechecks;
     unsigned long long dist_tests[8];  // distance tests evaluated, spread over 8 counters
-    long long reserved[3];
+    int reused;                // cores that joined a reused component this slide
+    int reuse_skip;            // slides left without forest reuse (it paid off too little)
+    long long reserved[2];
 };
 
 // Everything a kernel needs for one stream, passed by value.

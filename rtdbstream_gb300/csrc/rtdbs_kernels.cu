@@ -1029,6 +1029,11 @@ __global__ void __launch_bounds__(256) k_incr(View v, int j, int c, int init) {
 // as in a union from scratch.  Used with neighbour lists, where k_border
 // leaves the previous labels and ids by slot and resets the forest.
 
+// Reuse is skipped for 15 slides after a slide where fewer than 1 in 16 of
+// the window's points joined a reused component (streams whose expiries
+// touch every cluster), then tried again.
+constexpr int kReuseRetry = 15;
+
 // The slide's new slots: [base, base + S).
 __device__ __forceinline__ bool slot_is_new(const View& v, int s) {
     const int base = (int)(v.ctl->slide % v.units) * v.S;
@@ -1039,7 +1044,7 @@ __device__ __forceinline__ bool slot_is_new(const View& v, int s) {
 // the new points, read before the border pass overwrites them) and cores
 // now below MinPts.
 __device__ __forceinline__ void damage_body(const View& v, int bx, int nbx) {
-    if (!v.ctl->prev_ok) return;
+    if (!v.ctl->prev_ok || v.ctl->reuse_skip > 0) return;
     const int cur = (int)(v.ctl->b & 1);
     const int n = v.ctl->nocc[cur];
     const int* scnt = v.scnt[cur];
@@ -1060,11 +1065,12 @@ __device__ __forceinline__ void damage_body(const View& v, int bx, int nbx) {
 
 // Cores of intact components join their old root (parent and hint).
 __device__ __forceinline__ void reuse_body(const View& v, int bx, int nbx) {
-    if (!v.ctl->prev_ok) return;
+    if (!v.ctl->prev_ok || v.ctl->reuse_skip > 0) return;
     const int cur = (int)(v.ctl->b & 1);
     const int n = v.ctl->nocc[cur];
     const int* scnt = v.scnt[cur];
     const int* sw = reinterpret_cast<const int*>(v.spt[cur]) + 3;
+    unsigned reused = 0;
     for (int i = bx * blockDim.x + threadIdx.x; i < n; i += nbx * blockDim.x) {
         if (scnt[i] < v.min_pts) continue;
         const int s = sw[4 * (size_t)i];
@@ -1073,7 +1079,10 @@ __device__ __forceinline__ void reuse_body(const View& v, int bx, int nbx) {
         if (v.damaged[r]) continue;
         v.parent[s] = r;
         v.sroot[i] = r;
+        ++reused;
     }
+    reused = __reduce_add_sync(kFull, reused);
+    if ((threadIdx.x & 31) == 0 && reused) atomicAdd(&v.ctl->reused, (int)reused);
 }
 
 __global__ void k_damage(View v) { damage_body(v, blockIdx.x, gridDim.x); }
@@ -1406,6 +1415,13 @@ __device__ __forceinline__ void border_body(const View& v, int advance, int bx, 
     }
     if (bx == 0 && threadIdx.x == 0) {
         v.ctl->union_next = 0;                // the next clustering's queue; not read here
+        // k_damage / k_reuse of this clustering are done: judge the reuse
+        // (not after a fresh window, which had no previous forest)
+        if (v.ctl->reuse_skip > 0)
+            v.ctl->reuse_skip -= 1;
+        else if (v.ctl->prev_ok && v.ctl->reused < v.W / 16)
+            v.ctl->reuse_skip = kReuseRetry;
+        v.ctl->reused = 0;
         v.ctl->prev_ok = 1;                   // the forest of this clustering can be reused
         if (advance) v.ctl->slide += 1;       // no reader here
     }
