@@ -103,7 +103,10 @@ typedef struct rtdbs_stats {
     int32_t chunks_per_slide;   /* grid-update chunks per slide (ceil(S / 16384)) */
     int64_t dist_tests;         /* distance tests evaluated, cumulative (the reference's
                                    DEBUG_INFO num_dist_calculations, src/dbscan/dbscan.cpp:145-212) */
-    int64_t reserved[2];
+    int64_t reused_cores;       /* cores that started the last clustering in a component
+                                   kept from the previous slide (no counterpart in the
+                                   reference, which re-clusters every slide) */
+    int64_t reserved[1];
 } rtdbs_stats;
 
 /* Per-phase device time of one profiled slide, in milliseconds (the

@@ -544,6 +544,7 @@ int rtdbs_get_stats(rtdbs_engine* e, rtdbs_stats* s) {
     s->slides = e->h_ctl->slide;
     s->band_rechecks = (int64_t)e->h_ctl->band_rechecks;
     for (int k = 0; k < 8; ++k) s->dist_tests += (int64_t)e->h_ctl->dist_tests[k];
+    s->reused_cores = e->h_ctl->last_reused;
     s->cells = e->h_ctl->ncells;
     s->work_items = e->h_ctl->nitems;
     s->error_bits = e->h_ctl->err;

@@ -71,7 +71,8 @@ struct Ctl {
     unsigned long long dist_tests[8];  // distance tests evaluated, spread over 8 counters
     int reused;                // cores that joined a reused component this slide
     int reuse_skip;            // slides left without forest reuse (it paid off too little)
-    long long reserved[2];
+    long long last_reused;     // `reused` of the last clustering
+    long long reserved[1];
 };
 
 // Everything a kernel needs for one stream, passed by value.

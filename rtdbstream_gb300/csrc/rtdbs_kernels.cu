@@ -1421,6 +1421,7 @@ __device__ __forceinline__ void border_body(const View& v, int advance, int bx, 
             v.ctl->reuse_skip -= 1;
         else if (v.ctl->prev_ok && v.ctl->reused < v.W / 16)
             v.ctl->reuse_skip = kReuseRetry;
+        v.ctl->last_reused = v.ctl->reused;
         v.ctl->reused = 0;
         v.ctl->prev_ok = 1;                   // the forest of this clustering can be reused
         if (advance) v.ctl->slide += 1;       // no reader here

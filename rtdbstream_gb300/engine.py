@@ -54,7 +54,8 @@ class Stats(ctypes.Structure):
                 ("error_bits", ctypes.c_int32), ("key_bits", ctypes.c_int32),
                 ("cell_side", ctypes.c_double), ("device_bytes", ctypes.c_int64),
                 ("launches_per_slide", ctypes.c_int32), ("chunks_per_slide", ctypes.c_int32),
-                ("dist_tests", ctypes.c_int64), ("reserved", ctypes.c_int64 * 2)]
+                ("dist_tests", ctypes.c_int64), ("reused_cores", ctypes.c_int64),
+                ("reserved", ctypes.c_int64 * 1)]
 
 
 PHASES = ("ingest", "sort", "decrement", "merge", "build", "increment", "union", "flatten", "label")

@@ -223,3 +223,40 @@ def test_walkers_full_window_exact():
     got = run_stream(pts, spec.window, spec.stride, spec.eps, spec.min_pts, 2)
     exp = O.stream(pts, spec.window, spec.stride, spec.eps, spec.min_pts, O.MODE_FP64, first_slide=1, n_out=2)
     assert_same(got[:3], exp, "walkers 1M")
+
+
+def reuse_stream(seed=21):
+    """A window whose oldest points are far-away noise and a bridge between
+    two blobs, its newest points three stationary 2-D blobs: the first slides
+    expire only noise and bridge points, so blob components lose no core
+    (reused) while the bridged pair splits; new points land next to one blob
+    (insertions into a kept component) and in the noise region."""
+    rng = np.random.default_rng(seed)
+    W, S = 6_000, 500
+    noise = rng.uniform(50.0, 60.0, size=(1_500, 2))
+    bridge = np.stack([np.linspace(0.5, 9.5, 500), np.full(500, 0.0)], axis=1) + rng.normal(0, 0.01, (500, 2))
+    blobs = np.concatenate([rng.normal(c, 0.4, size=(1_334, 2)) for c in ((0.0, 0.0), (10.0, 0.0), (0.0, 10.0))])
+    blobs = blobs[rng.permutation(len(blobs))][: W - 2_000]
+    window = np.concatenate([noise, bridge, blobs])
+    new = np.concatenate([np.concatenate([rng.normal((0.0, 10.0), 0.4, size=(100, 2)),
+                                          rng.uniform(50.0, 60.0, size=(S - 100, 2))]) for _ in range(4)])
+    return np.concatenate([window, new]).astype(np.float32), W, S
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_forest_reuse_matches_oracle(precision):
+    pts, W, S = reuse_stream()
+    eps, mp = 0.25, 5
+    got = run_stream(pts, W, S, eps, mp, 4, precision=precision)
+    mode = O.MODE_FP64 if precision == "fp64" else O.MODE_FP32
+    exp = O.stream(pts, W, S, eps, mp, mode, first_slide=1, n_out=4)
+    assert_same(got[:3], exp, f"reuse/{precision}")
+    # the blob components were kept from the previous slide
+    assert got[3]["reused_cores"] > 1_000
+    # the bridge expired in the last slide: the two blobs it joined split
+    win = O.window_of(pts, W, S, 4)
+    lab, cid = got[1][-1], got[2][-1]
+    core = lab == 0
+    a = np.argmin(((win - (0.0, 0.0)) ** 2).sum(1) + np.where(core, 0.0, 1e9))
+    b = np.argmin(((win - (10.0, 0.0)) ** 2).sum(1) + np.where(core, 0.0, 1e9))
+    assert cid[a] != cid[b]
