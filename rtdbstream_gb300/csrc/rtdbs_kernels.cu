@@ -1108,7 +1108,7 @@ __device__ __forceinline__ void reuse_body(const View& v, int bx, int nbx) {
             }
         }
         v.sclass[i] = cls;
-        v.kclass[sw[4 * (size_t)i]] = cls;  // every slot: the window is full
+        if (cls) v.kclass[sw[4 * (size_t)i]] = cls;
     }
     reused = __reduce_add_sync(kFull, reused);
     if ((threadIdx.x & 31) == 0 && reused) atomicAdd(&v.ctl->reused, (int)reused);
