@@ -195,8 +195,7 @@ size_t plan_layout(rtdbs_engine* e, std::vector<Part>& parts) {
     const size_t list_ints = (size_t)W * v.list_stride;
     const size_t track_ints = v.list_cap >= 0 ? (size_t)W : 0;
     v.nlist = v.ntrack = v.rslot = v.damaged = nullptr;
-    v.sclass = v.kclass = nullptr;
-    v.tedge = nullptr;
+    v.sclass = nullptr;
     parts = {
         {(void**)&v.ring, sizeof(float4) * W},
         {(void**)&v.kslot, sizeof(unsigned long long) * W},
@@ -218,8 +217,6 @@ size_t plan_layout(rtdbs_engine* e, std::vector<Part>& parts) {
         {(void**)&v.rslot, sizeof(int) * track_ints},
         {(void**)&v.damaged, sizeof(int) * track_ints},
         {(void**)&v.sclass, track_ints},
-        {(void**)&v.kclass, track_ints},
-        {(void**)&v.tedge, sizeof(unsigned long long) * track_ints},
         {(void**)&v.nsort, sizeof(unsigned long long) * C},
         {(void**)&v.xsort, sizeof(unsigned long long) * C},
         {(void**)&v.nword, sizeof(unsigned long long) * C},
@@ -559,8 +556,8 @@ int rtdbs_get_stats(rtdbs_engine* e, rtdbs_stats* s) {
     const int nchunks = (e->p.stride + e->chunk - 1) / e->chunk;
     s->chunks_per_slide = nchunks;
     // sort phase = 2 kernels; with neighbour lists the union phase adds the
-    // four forest-reuse passes
-    s->launches_per_slide = nchunks * (rtdbs::kChunkPhases + 1) + 3 + (e->v.list_cap >= 0 ? 4 : 0);
+    // two forest-reuse passes
+    s->launches_per_slide = nchunks * (rtdbs::kChunkPhases + 1) + 3 + (e->v.list_cap >= 0 ? 2 : 0);
     return RTDBS_OK;
 }
 
@@ -1116,7 +1113,7 @@ int rtdbs_pool_slide_profiled(rtdbs_pool* p, int32_t n, const int32_t* ids, cons
     if (rc == RTDBS_OK) {
         // batch phases -> the engine's phase slots (sort + run merge are one)
         // (the forest-reuse passes belong to the union phase, as in the single-stream launch)
-        static const int slot[rtdbs::kNumBatchPhases] = {0, 1, 1, 2, 3, 4, 5, 6, 6, 6, 6, 6, 7, 8};
+        static const int slot[rtdbs::kNumBatchPhases] = {0, 1, 1, 2, 3, 4, 5, 6, 6, 6, 7, 8};
         float ph[9] = {0};
         for (size_t i = 0; i < p->plan.size(); ++i) {
             float ms = 0.f;

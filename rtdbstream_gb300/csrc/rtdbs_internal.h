@@ -23,8 +23,6 @@
 //   rslot  i32[W]         per slot after the flatten: root (core) or -1
 //   damaged i32[W]        per previous root: the component lost a core this slide
 //   sclass u8[W]          per sorted position: core class for the union (forest reuse)
-//   kclass u8[W]          the same by slot
-//   tedge  u64[W]         per slot: the core-core edge whose union hooked it (tree edges)
 //   ntrack i32[W]         1: the slot's list is exact; 0: not kept (core, or
 //                         rebuilt at the end of the slide)
 //   chunk scratch: sort words, expired points.
@@ -123,9 +121,6 @@ struct View {
                                  // slide (0 outside the union phase)
     unsigned char* sclass;       // per sorted position while reusing: 0 not core, 1 core
                                  // of a kept component, 2 core of a damaged one, 3 new core
-    unsigned char* kclass;       // the same class by slot
-    unsigned long long* tedge;   // per slot: the edge (two slots) whose union hooked this
-                                 // root; valid for every non-root core of the last clustering
     int* ntrack;                 // per slot: 1 list exact, 0 not kept
     unsigned long long* nsort;   // chunk sort words in (key << 14 | offset)
     unsigned long long* xsort;
@@ -177,8 +172,6 @@ enum BatchPhase : int {
     kBatchIncrement,
     kBatchDamage,
     kBatchReuse,
-    kBatchPrelink,
-    kBatchRehint,
     kBatchUnion,
     kBatchFlatten,
     kBatchLabel,

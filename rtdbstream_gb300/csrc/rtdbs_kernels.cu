@@ -329,11 +329,7 @@ __device__ __forceinline__ int uf_find(int* parent, int v) {
 // revealed.  max(a, b) falls every round, so the loop ends, and parents only
 // ever point to smaller slots, so every root is the minimum slot of its set.
 // Returns an ancestor of both points afterwards.
-// With `tedge`, the root that a successful CAS hooks records `edge` (the two
-// adjacent core slots whose union it is), so the recorded edges of the
-// non-root cores form a spanning forest of real core-core edges.
-__device__ __forceinline__ int uf_hook(int* parent, int a, int b, int& err,
-                                       unsigned long long* tedge = nullptr, unsigned long long edge = 0) {
+__device__ __forceinline__ int uf_hook(int* parent, int a, int b, int& err) {
     for (int it = 0; it < kMaxIter; ++it) {
         if (a == b) return a;
         if (a < b) {
@@ -342,18 +338,11 @@ __device__ __forceinline__ int uf_hook(int* parent, int a, int b, int& err,
             b = t;
         }
         const int old = atomicCAS(&parent[a], a, b);
-        if (old == a) {
-            if (tedge) tedge[a] = edge;
-            return b;
-        }
+        if (old == a) return b;
         a = uf_find(parent, old);
     }
     err |= kErrUnionIter;
     return a < b ? a : b;
-}
-
-__device__ __forceinline__ unsigned long long edge_of(int x, int y) {
-    return ((unsigned long long)(unsigned)x << 32) | (unsigned)y;
 }
 
 __device__ __forceinline__ void flush_stats(const View& v, const Tally& t, int err, int lane) {
@@ -1108,53 +1097,11 @@ __device__ __forceinline__ void reuse_body(const View& v, int bx, int nbx) {
             }
         }
         v.sclass[i] = cls;
-        if (cls) v.kclass[sw[4 * (size_t)i]] = cls;
     }
     reused = __reduce_add_sync(kFull, reused);
     if ((threadIdx.x & 31) == 0 && reused) atomicAdd(&v.ctl->reused, (int)reused);
 }
 
-// Cores of damaged components start alone, but most of their old tree
-// edges survive: the recorded edge of every such core (a non-root of the
-// previous clustering) is linked again when both its ends are still cores
-// of a damaged component (neither expired nor fell below MinPts), which is
-// a real edge of the new core graph.  Only connections through lost cores
-// are then left for the union's scan.
-__device__ __forceinline__ void prelink_body(const View& v, int bx, int nbx) {
-    if (!v.ctl->reuse_on) return;
-    const int cur = (int)(v.ctl->b & 1);
-    const int n = v.ctl->nocc[cur];
-    const int* sw = reinterpret_cast<const int*>(v.spt[cur]) + 3;
-    int err = 0;
-    for (int i = bx * blockDim.x + threadIdx.x; i < n; i += nbx * blockDim.x) {
-        if (v.sclass[i] != 2) continue;
-        const int a = sw[4 * (size_t)i];
-        if (v.cid[a] == a) continue;  // an old root: no recorded edge
-        const unsigned long long e = v.tedge[a];
-        const int x = (int)(e >> 32), y = (int)(unsigned)e;
-        if (x < 0 || x >= v.W || y < 0 || y >= v.W) {
-            err |= kErrChunk;
-            continue;
-        }
-        if (v.kclass[x] != 2 || v.kclass[y] != 2) continue;
-        uf_hook(v.parent, uf_find(v.parent, x), uf_find(v.parent, y), err, v.tedge, e);
-    }
-    if (err) atomicOr(&v.ctl->err, err);
-}
-
-// Root hints of the re-linked cores: their roots after the pre-link, so the
-// union skips pairs inside a re-linked piece.
-__device__ __forceinline__ void rehint_body(const View& v, int bx, int nbx) {
-    if (!v.ctl->reuse_on) return;
-    const int cur = (int)(v.ctl->b & 1);
-    const int n = v.ctl->nocc[cur];
-    const int* sw = reinterpret_cast<const int*>(v.spt[cur]) + 3;
-    for (int i = bx * blockDim.x + threadIdx.x; i < n; i += nbx * blockDim.x)
-        if (v.sclass[i] == 2) v.sroot[i] = uf_find(v.parent, sw[4 * (size_t)i]);
-}
-
-__global__ void k_prelink(View v) { prelink_body(v, blockIdx.x, gridDim.x); }
-__global__ void k_rehint(View v) { rehint_body(v, blockIdx.x, gridDim.x); }
 __global__ void k_damage(View v) { damage_body(v, blockIdx.x, gridDim.x); }
 __global__ void k_reuse(View v) { reuse_body(v, blockIdx.x, gridDim.x); }
 
@@ -1274,7 +1221,7 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
                     adj &= adj - 1;
                     const int ra = rh[hi];
                     if (ra != rq) {
-                        rq = uf_hook(parent, ra, rq, err, v.tedge, edge_of(slot_of(hpt[hi]), slot_of(q)));
+                        rq = uf_hook(parent, ra, rq, err);
                         rh[hi] = rq;  // an ancestor of both points (benign race)
                     }
                 }
@@ -1534,8 +1481,6 @@ template <> struct PhaseShape<kBatchBuild> { static constexpr int threads = kBui
 template <> struct PhaseShape<kBatchIncrement> { static constexpr int threads = 256, min_blocks = 8; };
 template <> struct PhaseShape<kBatchDamage> { static constexpr int threads = 256, min_blocks = 1; };
 template <> struct PhaseShape<kBatchReuse> { static constexpr int threads = 256, min_blocks = 1; };
-template <> struct PhaseShape<kBatchPrelink> { static constexpr int threads = 256, min_blocks = 1; };
-template <> struct PhaseShape<kBatchRehint> { static constexpr int threads = 256, min_blocks = 1; };
 template <> struct PhaseShape<kBatchUnion> { static constexpr int threads = kClusterThreads, min_blocks = 8; };
 template <> struct PhaseShape<kBatchFlatten> { static constexpr int threads = 256, min_blocks = 6; };
 template <> struct PhaseShape<kBatchLabel> { static constexpr int threads = kClusterThreads, min_blocks = 6; };
@@ -1599,10 +1544,6 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
         if (sv.list_cap >= 0) damage_body(sv, bx, nbx);
     } else if constexpr (PHASE == kBatchReuse) {
         if (sv.list_cap >= 0) reuse_body(sv, bx, nbx);
-    } else if constexpr (PHASE == kBatchPrelink) {
-        if (sv.list_cap >= 0) prelink_body(sv, bx, nbx);
-    } else if constexpr (PHASE == kBatchRehint) {
-        if (sv.list_cap >= 0) rehint_body(sv, bx, nbx);
     } else if constexpr (PHASE == kBatchUnion) {
         __shared__ ClusterSmem sm;
         union_body<MODE, DIM>(sv, sm);
@@ -1697,8 +1638,6 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
                 const int rb = max(1, min(sms0 * 8, (v.W + 255) / 256));
                 k_damage<<<rb, 256, 0, s>>>(v);
                 k_reuse<<<rb, 256, 0, s>>>(v);
-                k_prelink<<<rb, 256, 0, s>>>(v);
-                k_rehint<<<rb, 256, 0, s>>>(v);
             }
             const int sms = g_num_sms > 0 ? g_num_sms : 152;
             const int per_block = kClusterThreads / 32;
@@ -1761,9 +1700,7 @@ int batch_blocks(int phase, const View& v, int c) {
         case kBatchMerge: return (v.W + kMergeTile - 1) / kMergeTile;
         case kBatchBuild: return (v.W + kBuildThreads - 1) / kBuildThreads;
         case kBatchDamage:
-        case kBatchReuse:
-        case kBatchPrelink:
-        case kBatchRehint: return v.list_cap >= 0 ? max(1, min(1024, (v.W + 2047) / 2048)) : 0;
+        case kBatchReuse: return v.list_cap >= 0 ? max(1, min(1024, (v.W + 2047) / 2048)) : 0;
         case kBatchUnion: return max(1, min(1024, (v.W + 1023) / 1024));  // persistent, queue-fed
         case kBatchLabel:
             if (v.list_cap >= 0) return max(1, min(1024, (v.W + 1023) / 1024));  // k_border
@@ -1808,8 +1745,6 @@ cudaError_t launch_batch(int phase, int prec, int dim, const BatchLaunch& L, int
         case kBatchIncrement: RTDBS_BATCH_MD(kBatchIncrement, total_blocks, t, s); break;
         case kBatchDamage: k_batch<kBatchDamage, 0, 0><<<total_blocks, t, 0, s>>>(L); break;
         case kBatchReuse: k_batch<kBatchReuse, 0, 0><<<total_blocks, t, 0, s>>>(L); break;
-        case kBatchPrelink: k_batch<kBatchPrelink, 0, 0><<<total_blocks, t, 0, s>>>(L); break;
-        case kBatchRehint: k_batch<kBatchRehint, 0, 0><<<total_blocks, t, 0, s>>>(L); break;
         case kBatchUnion: RTDBS_BATCH_MD(kBatchUnion, total_blocks, t, s); break;
         case kBatchFlatten: RTDBS_BATCH_MD(kBatchFlatten, total_blocks, t, s); break;
         case kBatchLabel: RTDBS_BATCH_MD(kBatchLabel, total_blocks, t, s); break;
