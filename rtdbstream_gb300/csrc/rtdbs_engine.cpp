@@ -195,7 +195,6 @@ size_t plan_layout(rtdbs_engine* e, std::vector<Part>& parts) {
     const size_t list_ints = (size_t)W * v.list_stride;
     const size_t track_ints = v.list_cap >= 0 ? (size_t)W : 0;
     v.nlist = v.ntrack = v.rslot = v.damaged = nullptr;
-    v.sclass = nullptr;
     parts = {
         {(void**)&v.ring, sizeof(float4) * W},
         {(void**)&v.kslot, sizeof(unsigned long long) * W},
@@ -216,7 +215,6 @@ size_t plan_layout(rtdbs_engine* e, std::vector<Part>& parts) {
         {(void**)&v.ntrack, sizeof(int) * track_ints},
         {(void**)&v.rslot, sizeof(int) * track_ints},
         {(void**)&v.damaged, sizeof(int) * track_ints},
-        {(void**)&v.sclass, track_ints},
         {(void**)&v.nsort, sizeof(unsigned long long) * C},
         {(void**)&v.xsort, sizeof(unsigned long long) * C},
         {(void**)&v.nword, sizeof(unsigned long long) * C},

@@ -22,7 +22,6 @@
 //                         of 4 for 16-byte loads; -1 = empty entry)
 //   rslot  i32[W]         per slot after the flatten: root (core) or -1
 //   damaged i32[W]        per previous root: the component lost a core this slide
-//   sclass u8[W]          per sorted position: core class for the union (forest reuse)
 //   ntrack i32[W]         1: the slot's list is exact; 0: not kept (core, or
 //                         rebuilt at the end of the slide)
 //   chunk scratch: sort words, expired points.
@@ -71,10 +70,9 @@ struct Ctl {
     unsigned long long band_rechecks;
     unsigned long long dist_tests[8];  // distance tests evaluated, spread over 8 counters
     int reused;                // cores that joined a reused component this slide
-    int reuse_on;              // this clustering classified its cores (View::sclass)
     int reuse_skip;            // slides left without forest reuse (it paid off too little)
     long long last_reused;     // `reused` of the last clustering
-    int pad1;
+    long long reserved[1];
 };
 
 // Everything a kernel needs for one stream, passed by value.
@@ -119,8 +117,6 @@ struct View {
     int* rslot;                  // per slot: root of a core, -1 otherwise
     int* damaged;                // per old root slot: its component lost a core this
                                  // slide (0 outside the union phase)
-    unsigned char* sclass;       // per sorted position while reusing: 0 not core, 1 core
-                                 // of a kept component, 2 core of a damaged one, 3 new core
     int* ntrack;                 // per slot: 1 list exact, 0 not kept
     unsigned long long* nsort;   // chunk sort words in (key << 14 | offset)
     unsigned long long* xsort;

@@ -1044,9 +1044,7 @@ __device__ __forceinline__ bool slot_is_new(const View& v, int s) {
 // the new points, read before the border pass overwrites them) and cores
 // now below MinPts.
 __device__ __forceinline__ void damage_body(const View& v, int bx, int nbx) {
-    const bool on = v.ctl->prev_ok && v.ctl->reuse_skip == 0;
-    if (bx == 0 && threadIdx.x == 0) v.ctl->reuse_on = on ? 1 : 0;  // read from k_union on
-    if (!on) return;
+    if (!v.ctl->prev_ok || v.ctl->reuse_skip > 0) return;
     const int cur = (int)(v.ctl->b & 1);
     const int n = v.ctl->nocc[cur];
     const int* scnt = v.scnt[cur];
@@ -1065,12 +1063,7 @@ __device__ __forceinline__ void damage_body(const View& v, int bx, int nbx) {
     }
 }
 
-// Cores of intact components join their old root (parent and hint), and
-// every position gets its class for the union: a kept core's core
-// neighbours are kept cores of its own component or new cores (adjacent old
-// cores were in one old component), so work items whose cores are all kept
-// have nothing to join and are skipped, and the edges of a kept core to a
-// new core are found from the new core's side.
+// Cores of intact components join their old root (parent and hint).
 __device__ __forceinline__ void reuse_body(const View& v, int bx, int nbx) {
     if (!v.ctl->prev_ok || v.ctl->reuse_skip > 0) return;
     const int cur = (int)(v.ctl->b & 1);
@@ -1079,24 +1072,14 @@ __device__ __forceinline__ void reuse_body(const View& v, int bx, int nbx) {
     const int* sw = reinterpret_cast<const int*>(v.spt[cur]) + 3;
     unsigned reused = 0;
     for (int i = bx * blockDim.x + threadIdx.x; i < n; i += nbx * blockDim.x) {
-        unsigned char cls = 0;
-        if (scnt[i] >= v.min_pts) {
-            const int s = sw[4 * (size_t)i];
-            if (v.label[s] != 0 || slot_is_new(v, s)) {
-                cls = 3;
-            } else {
-                const int r = v.cid[s];
-                if (v.damaged[r]) {
-                    cls = 2;
-                } else {
-                    cls = 1;
-                    v.parent[s] = r;
-                    v.sroot[i] = r;
-                    ++reused;
-                }
-            }
-        }
-        v.sclass[i] = cls;
+        if (scnt[i] < v.min_pts) continue;
+        const int s = sw[4 * (size_t)i];
+        if (v.label[s] != 0 || slot_is_new(v, s)) continue;
+        const int r = v.cid[s];
+        if (v.damaged[r]) continue;
+        v.parent[s] = r;
+        v.sroot[i] = r;
+        ++reused;
     }
     reused = __reduce_add_sync(kFull, reused);
     if ((threadIdx.x & 31) == 0 && reused) atomicAdd(&v.ctl->reused, (int)reused);
@@ -1140,9 +1123,6 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
     // each to the point's own slot): coalesced with the candidate loads, and
     // refreshed as roots are found, so find walks stay short.
     volatile int* hint = v.sroot;
-    // Core classes of the forest reuse (see reuse_body): items whose cores
-    // are all kept are skipped; items with a new core scan the full stencil.
-    const bool classes = v.ctl->reuse_on != 0;
     Tally tally;
     int err = 0;
     // Warps take batches of kBatch consecutive work items (neighbouring
@@ -1162,16 +1142,12 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
         const bool hv = lane < len;
         float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
         bool hcore = false;
-        int hcls = 2;
         if (hv) {
             h = spt[start + lane];
             hcore = scnt[start + lane] >= v.min_pts;
-            if (classes) hcls = v.sclass[start + lane];
         }
         const unsigned hmask = __ballot_sync(kFull, hcore);
         if (!hmask) continue;
-        if (!__any_sync(kFull, hcore && hcls >= 2)) continue;  // every core kept: nothing to join
-        const bool full = __any_sync(kFull, hcore && hcls == 3);
         __syncwarp();
         const int hh = hcore ? hint[start + lane] : 0;
         if (hcore) rh[lane] = hh;
@@ -1182,14 +1158,9 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
         const int r0 = __shfl_sync(kFull, hh, __ffs(hmask) - 1);
         const bool uni = __all_sync(kFull, !hcore || hh == r0);
         const int hmin = start + __ffs(hmask) - 1;
-        int rs, re, total;
-        if (full) {  // a new core: its pairs with kept cores below it are found here
-            row_ranges<DIM, false>(v, T, gen, skey[start], lane, rs, re);
-            total = candidate_stream<Stencil<DIM, false>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
-        } else {
-            row_ranges<DIM, true>(v, T, gen, skey[start], lane, rs, re);
-            total = candidate_stream<Stencil<DIM, true>::kRows>(rs, re, hmin + 1, lane, rstart[wib], rpre[wib]);
-        }
+        int rs, re;
+        row_ranges<DIM, true>(v, T, gen, skey[start], lane, rs, re);
+        const int total = candidate_stream<Stencil<DIM, true>::kRows>(rs, re, hmin + 1, lane, rstart[wib], rpre[wib]);
         int r = 0;
         for (int base = 0; base < total; base += 32) {
             const int idx = base + lane;
@@ -1210,8 +1181,7 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
             while (mm) {
                 const int hi = __ffs(mm) - 1;
                 mm &= mm - 1;
-                if (qc && (full ? pos != start + hi : pos > start + hi) && qh != rh[hi] &&
-                    is_nbr<MODE, DIM>(v, hpt[hi], q, tally))
+                if (qc && pos > start + hi && qh != rh[hi] && is_nbr<MODE, DIM>(v, hpt[hi], q, tally))
                     adj |= 1u << hi;
             }
             if (adj) {
