@@ -86,7 +86,13 @@ typedef struct rtdbs_params {
     float   bbox_max[3];
     int32_t device;       /* CUDA device ordinal */
     int32_t flags;        /* RTDBS_FLAG_* */
-    int32_t reserved[6];
+    int32_t cell_mult;    /* K: grid cells per Eps along each axis, 1 or 2 (0 = 1); the
+                             scan covers (2K+1)^dim cells of side Eps/K, so K = 2 tests
+                             fewer pairs where cells are dense and costs more cells and
+                             work items where they are sparse (rtdbstream_gb300/autotune.py
+                             picks it per stream).  The reference's grid has side Eps/sqrt(3)
+                             (src/dbscan/dbscan.cpp:34-37) */
+    int32_t reserved[5];
 } rtdbs_params;
 
 /* Cumulative counters (src/dbscan/dbscan.cpp:145-212 keeps similar debug counters). */

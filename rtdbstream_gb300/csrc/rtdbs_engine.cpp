@@ -94,14 +94,16 @@ struct rtdbs_engine {
 
 namespace {
 
-// Grid geometry: cell side L = Eps (1 + 2^-12) >= Eps (the margin covers the
-// rounding of both predicates and of the double cell coordinate), clamped
+// Grid geometry: cell side L = Eps (1 + 2^-12) / K with K cells per Eps (the
+// margin covers the rounding of both predicates and of the double cell
+// coordinate, so neighbours are at most K cells apart per axis), clamped
 // extents over the bounding box, one bit field per axis in the key, L doubled
 // until the fields fit 50 bits.
 int set_geometry(rtdbs_engine* e, const float* bmin, const float* bmax, bool widen) {
     const int dim = e->p.dim;
     double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-    double L = e->p.eps * (1.0 + 1.0 / 4096.0);
+    const int K = e->p.cell_mult > 0 ? e->p.cell_mult : 1;
+    double L = e->p.eps * (1.0 + 1.0 / 4096.0) / K;  // K cells per Eps: neighbours within K cells
     for (int a = 0; a < dim; ++a) {
         lo[a] = bmin[a];
         hi[a] = bmax[a];
@@ -355,6 +357,8 @@ int rtdbs_create(const rtdbs_params* params, void* cuda_stream, rtdbs_engine** o
     if (!(p.eps > 0.0) || !std::isfinite(p.eps)) return fail(RTDBS_ERR_INVALID, "eps must be finite and > 0");
     if (p.precision != RTDBS_PREC_FP64 && p.precision != RTDBS_PREC_FP32)
         return fail(RTDBS_ERR_INVALID, "unknown precision mode %d", p.precision);
+    if (p.cell_mult < 0 || p.cell_mult > 2)
+        return fail(RTDBS_ERR_INVALID, "cell_mult must be 0 (default), 1 or 2 (got %d)", p.cell_mult);
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(RTDBS_ERR_NO_DEVICE, "no CUDA device available");
@@ -379,6 +383,7 @@ int rtdbs_create(const rtdbs_params* params, void* cuda_stream, rtdbs_engine** o
     }
     View& v = e->v;
     v.dim = p.dim;
+    v.cell_mult = p.cell_mult > 0 ? p.cell_mult : 1;
     v.W = p.window;
     v.S = p.stride;
     v.min_pts = p.min_pts;
@@ -727,7 +732,7 @@ int pool_build_shape(rtdbs_pool* p, const std::vector<int>& ids) {
         if (rtdbs::batch_phase_split(ph)) {
             for (const auto& it : items) {
                 const auto& v = p->eng[it.view]->v;
-                const std::pair<int, int> g(v.precision, v.dim);
+                const std::pair<int, int> g(v.precision, rtdbs::dk_of(v));
                 if (std::find(groups.begin(), groups.end(), g) == groups.end()) groups.push_back(g);
             }
         } else {
@@ -737,7 +742,7 @@ int pool_build_shape(rtdbs_pool* p, const std::vector<int>& ids) {
             std::vector<BatchItem> sel;
             for (const auto& it : items) {
                 const auto& v = p->eng[it.view]->v;
-                if (!rtdbs::batch_phase_split(ph) || (v.precision == g.first && v.dim == g.second))
+                if (!rtdbs::batch_phase_split(ph) || (v.precision == g.first && rtdbs::dk_of(v) == g.second))
                     sel.push_back(it);
             }
             std::vector<int> prefix(sel.size() + 1, 0);

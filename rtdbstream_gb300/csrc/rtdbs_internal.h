@@ -84,6 +84,7 @@ struct View {
     long long ext[3];
     int shift[3];
     int dim;
+    int cell_mult;              // K: cells per Eps along each axis (1 or 2)
     // parameters
     int W, S, min_pts, units;   // units = W / S
     int chunk;                  // C
@@ -126,6 +127,9 @@ struct View {
     const float* staging;        // new points [S][dim]
     Ctl* ctl;
 };
+
+// Combined template code of a stream's work kernels: dim + 4 (cells per Eps - 1).
+__host__ __device__ inline int dk_of(const View& v) { return v.dim + 4 * (v.cell_mult - 1); }
 
 // Kernel phases of a slide, in launch order.
 enum Phase : int {
@@ -195,6 +199,7 @@ int batch_blocks(int phase, const View& v, int c);
 int batch_threads(int phase);
 // Phases launched once per (precision, dim) group of streams (the others
 // take every stream in one launch; prec and dim are then ignored).
+// `dim` here is the stream group's dk_of code (dimension and cells per Eps).
 bool batch_phase_split(int phase);
 cudaError_t launch_batch(int phase, int prec, int dim, const BatchLaunch& L, int total_blocks, int max_c,
                          cudaStream_t s);

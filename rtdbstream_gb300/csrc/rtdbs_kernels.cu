@@ -50,6 +50,7 @@ constexpr int kPrecFp32 = 1;
 
 __device__ __forceinline__ int slot_of(const float4& p) { return __float_as_int(p.w); }
 
+
 __device__ __forceinline__ unsigned lanemask_lt(int lane) { return (1u << lane) - 1u; }
 
 // ------------------------------------------------------------------ geometry
@@ -191,30 +192,39 @@ __device__ bool table_set(ulonglong2* T, unsigned pmask, int pbits, unsigned lon
     return false;
 }
 
-// Rows of the 3^DIM stencil: the cells (last axis -1, 0, +1) of one row have
-// consecutive keys, so a row is one contiguous range of the cell-sorted
-// window.  The full stencil has 3^(DIM-1) rows.  The upper half (HALF) keeps
-// only the rows whose keys are not below the home cell's -- the centre row
-// (without its -1 cell) and the rows after it in key order -- since every
-// position below the home cell is clipped away by a pair-once union anyway.
-template <int DIM, bool HALF>
+// Rows of the stencil.  With K cells per Eps along each axis (cell side
+// Eps (1 + 2^-12) / K) a point's neighbours lie within K cells per axis, in
+// the (2K+1)^DIM cells around its own.  The 2K+1 cells of one row (last axis
+// -K..K) have consecutive keys, so a row is one contiguous range of the
+// cell-sorted window; the full stencil has (2K+1)^(DIM-1) rows.  The upper
+// half (HALF) keeps only the rows whose keys are not below the home cell's --
+// the centre row (without its negative cells) and the rows after it in key
+// order -- since every position below the home cell is clipped away by a
+// pair-once union anyway.
+//
+// The work kernels take a combined template parameter DK = DIM + 4 (K - 1):
+// DK 1..3 for one cell per Eps, 5..7 for two.
+template <int DIM, bool HALF, int K = 1>
 struct Stencil {
-    static constexpr int kAllRows = DIM == 1 ? 1 : (DIM == 2 ? 3 : 9);
+    static constexpr int kW = 2 * K + 1;  // cells per row
+    static constexpr int kAllRows = DIM == 1 ? 1 : (DIM == 2 ? kW : kW * kW);
     static constexpr int kFirst = HALF ? (kAllRows - 1) / 2 : 0;  // first row kept
     static constexpr int kRows = kAllRows - kFirst;
 };
+constexpr int kMaxRows = 25;  // (2K+1)^2 rows for K = 2 in 3-D
 
 // Row ranges of the stencil around `key`, computed by a group of G lanes
 // (the whole warp, or each 16-lane half for its own key; `lane` counts within
-// the group; a lane looks up one or two cells).  On return group lane
+// the group; a lane looks up one to four cells).  On return group lane
 // r < kRows holds row r as [rs, re) (empty rows: rs == re).
-template <int DIM, bool HALF, int G = 32>
+template <int DIM, bool HALF, int K = 1, int G = 32>
 __device__ __forceinline__ void row_ranges(const View& v, const ulonglong2* T, unsigned gen,
                                            unsigned long long key, int lane, int& rs, int& re) {
-    using St = Stencil<DIM, HALF>;
-    constexpr int kSlots = 3 * St::kRows;            // cell slots, kept row by kept row
+    using St = Stencil<DIM, HALF, K>;
+    constexpr int kW = St::kW;
+    constexpr int kSlots = kW * St::kRows;           // cell slots, kept row by kept row
     constexpr int kPer = (kSlots + G - 1) / G;       // cells per lane
-    static_assert(kPer <= 2, "stencil too large for the lane group");
+    static_assert(kPer <= 4 && St::kRows <= G, "stencil too large for the lane group");
     const long long c2 = (long long)(key & ((1ull << v.shift[1]) - 1ull));
     const long long c1 = (long long)((key >> v.shift[1]) & ((1ull << (v.shift[0] - v.shift[1])) - 1ull));
     const long long c0 = (long long)(key >> v.shift[0]);
@@ -222,19 +232,19 @@ __device__ __forceinline__ void row_ranges(const View& v, const ulonglong2* T, u
 #pragma unroll
     for (int k = 0; k < kPer; ++k) {
         rg[k] = make_int2(0, 0);
-        const int cs = lane + k * G;                                  // = 3 * kept row + cell
-        const int row = St::kFirst + cs / 3, d_last = cs % 3 - 1;
-        const bool skip = HALF && cs < 3 && d_last < 0;              // centre row, cell -1
+        const int cs = lane + k * G;                                  // = kW * kept row + cell
+        const int row = St::kFirst + cs / kW, d_last = cs % kW - K;
+        const bool skip = HALF && cs < kW && d_last < 0;             // centre row, negative cells
         if (cs < kSlots && !skip) {
             long long q0 = c0, q1 = c1, q2 = c2;
             if (DIM == 1) {
                 q0 += d_last;
             } else if (DIM == 2) {
-                q0 += row - 1;
+                q0 += row - K;
                 q1 += d_last;
             } else {
-                q0 += row / 3 - 1;
-                q1 += row % 3 - 1;
+                q0 += row / kW - K;
+                q1 += row % kW - K;
                 q2 += d_last;
             }
             const bool ok = q0 >= 0 && q0 < v.ext[0] && q1 >= 0 && q1 < v.ext[1] && q2 >= 0 && q2 < v.ext[2];
@@ -247,17 +257,17 @@ __device__ __forceinline__ void row_ranges(const View& v, const ulonglong2* T, u
     }
     int s = INT_MAX, e = INT_MIN;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const int cs = min(3 * lane + k, kSlots - 1);   // slot of row `lane`'s cell k
+    for (int k = 0; k < kW; ++k) {
+        const int cs = min(kW * lane + k, kSlots - 1);   // slot of row `lane`'s cell k
         const int src = cs % G, which = cs / G;
-        int a = __shfl_sync(kFull, rg[0].x, src, G);
-        int b = __shfl_sync(kFull, rg[0].y, src, G);
-        if (kPer > 1) {
-            const int a1 = __shfl_sync(kFull, rg[kPer - 1].x, src, G);
-            const int b1 = __shfl_sync(kFull, rg[kPer - 1].y, src, G);
-            if (which) {
-                a = a1;
-                b = b1;
+        int a = 0, b = 0;
+#pragma unroll
+        for (int w = 0; w < kPer; ++w) {
+            const int aw = __shfl_sync(kFull, rg[w].x, src, G);
+            const int bw = __shfl_sync(kFull, rg[w].y, src, G);
+            if (w == which) {
+                a = aw;
+                b = bw;
             }
         }
         if (b > a) {
@@ -282,7 +292,7 @@ __device__ __forceinline__ int candidate_stream(int rs, int re, int lo, int lane
     const int len = lane < ROWS ? max(re - a, 0) : 0;
     int incl = len;
 #pragma unroll
-    for (int o = 1; o < 16; o <<= 1) {
+    for (int o = 1; o < (ROWS > 16 ? 32 : 16); o <<= 1) {
         const int t = __shfl_up_sync(kFull, incl, o, G);
         if (lane >= o) incl += t;
     }
@@ -581,28 +591,30 @@ __global__ void __launch_bounds__(kSortRun) k_runmerge(View v, int c, int init) 
 }
 
 // -1 on the count of every surviving neighbour of each expired point (old grid).
-// Points a count pass gives each warp: 1 (32 lanes each) or 2 (one per
-// 16-lane half), so two queries' dependent loads overlap.
+// Lanes a count pass gives each query point: 16 (two points per warp, so
+// two queries' dependent loads overlap) with one cell per Eps; the 25 rows of
+// the two-cells-per-Eps stencil need the whole warp.
 constexpr int kQueryLanes = 16;
-constexpr int kQueriesPerWarp = 32 / kQueryLanes;
+__host__ __device__ constexpr int query_lanes(int k) { return k == 1 ? kQueryLanes : 32; }
 
 struct StreamSmem {
-    int rstart[8][9], rpre[8][10];
-    int grstart[8][2][9], grpre[8][2][10];  // per 16-lane group (count passes)
+    int rstart[8][kMaxRows], rpre[8][kMaxRows + 1];
+    int grstart[8][2][kMaxRows], grpre[8][2][kMaxRows + 1];  // per lane group (count passes)
     int nbuf[8][kListCap];
     int gnbuf[8][2][kListCap];
     int queue[256];  // k_flatten: positions whose lists are rebuilt, in the block's tile
     int nq;
 };
 
-template <int MODE, int DIM>
+template <int MODE, int DK>
 __device__ __forceinline__ void decr_body(const View& v, int j, int c, int bx, StreamSmem& sm) {
-    constexpr int G = kQueryLanes;
+    constexpr int DIM = DK & 3, K = (DK >> 2) + 1;  // dimension, cells per Eps
+    constexpr int G = query_lanes(K), kPerWarp = 32 / G;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int grp = lane / G, gl = lane % G;
     const int gw = (bx * blockDim.x + threadIdx.x) >> 5;
-    if (gw * kQueriesPerWarp >= c) return;
-    const int qi = gw * kQueriesPerWarp + grp;
+    if (gw * kPerWarp >= c) return;
+    const int qi = gw * kPerWarp + grp;
     const bool has = qi < c;
     int* rstart = sm.grstart[wib][grp];
     int* rpre = sm.grpre[wib][grp];
@@ -614,8 +626,8 @@ __device__ __forceinline__ void decr_body(const View& v, int j, int c, int bx, S
     const unsigned long long key = word >> kOffBits;
     const float4 xp = has ? v.xpt[word & ((1u << kOffBits) - 1)] : make_float4(0.f, 0.f, 0.f, 0.f);
     int rs, re;
-    row_ranges<DIM, false, G>(v, v.table[old], gen, key, gl, rs, re);
-    int total = candidate_stream<Stencil<DIM, false>::kRows, G>(rs, re, 0, gl, rstart, rpre);
+    row_ranges<DIM, false, K, G>(v, v.table[old], gen, key, gl, rs, re);
+    int total = candidate_stream<Stencil<DIM, false, K>::kRows, G>(rs, re, 0, gl, rstart, rpre);
     if (!has) total = 0;
     const float4* spt = v.spt[old];
     int* scnt = v.scnt[old];
@@ -636,10 +648,10 @@ __device__ __forceinline__ void decr_body(const View& v, int j, int c, int bx, S
     flush_stats(v, tally, 0, lane);
 }
 
-template <int MODE, int DIM>
+template <int MODE, int DK>
 __global__ void __launch_bounds__(256) k_decr(View v, int j, int c) {
     __shared__ StreamSmem sm;
-    decr_body<MODE, DIM>(v, j, c, blockIdx.x, sm);
+    decr_body<MODE, DK>(v, j, c, blockIdx.x, sm);
 }
 
 __device__ __forceinline__ bool tuple_less(unsigned long long ka, int sa, unsigned long long kb,
@@ -941,14 +953,15 @@ __global__ void __launch_bounds__(kBuildThreads) k_build(View v) {
 }
 
 // Full count of each new point and +1 on every older neighbour (new grid).
-template <int MODE, int DIM>
+template <int MODE, int DK>
 __device__ __forceinline__ void incr_body(const View& v, int j, int c, int init, int bx, StreamSmem& sm) {
-    constexpr int G = kQueryLanes;
+    constexpr int DIM = DK & 3, K = (DK >> 2) + 1;  // dimension, cells per Eps
+    constexpr int G = query_lanes(K), kPerWarp = 32 / G;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int grp = lane / G, gl = lane % G;
     const int gw = (bx * blockDim.x + threadIdx.x) >> 5;
-    if (gw * kQueriesPerWarp >= c) return;
-    const int qi = gw * kQueriesPerWarp + grp;
+    if (gw * kPerWarp >= c) return;
+    const int qi = gw * kPerWarp + grp;
     const bool has = qi < c;
     int* rstart = sm.grstart[wib][grp];
     int* rpre = sm.grpre[wib][grp];
@@ -961,8 +974,8 @@ __device__ __forceinline__ void incr_body(const View& v, int j, int c, int init,
     const int aslot = el + (int)(word & ((1u << kOffBits) - 1));
     const float4 ap = has ? v.ring[aslot] : make_float4(0.f, 0.f, 0.f, 0.f);
     int rs, re;
-    row_ranges<DIM, false, G>(v, v.table[cur], gen, key, gl, rs, re);
-    int total = candidate_stream<Stencil<DIM, false>::kRows, G>(rs, re, 0, gl, rstart, rpre);
+    row_ranges<DIM, false, K, G>(v, v.table[cur], gen, key, gl, rs, re);
+    int total = candidate_stream<Stencil<DIM, false, K>::kRows, G>(rs, re, 0, gl, rstart, rpre);
     if (!has) total = 0;
     int tmax = total;
 #pragma unroll
@@ -1012,10 +1025,10 @@ __device__ __forceinline__ void incr_body(const View& v, int j, int c, int init,
     flush_stats(v, tally, err, lane);
 }
 
-template <int MODE, int DIM>
+template <int MODE, int DK>
 __global__ void __launch_bounds__(256) k_incr(View v, int j, int c, int init) {
     __shared__ StreamSmem sm;
-    incr_body<MODE, DIM>(v, j, c, init, blockIdx.x, sm);
+    incr_body<MODE, DK>(v, j, c, init, blockIdx.x, sm);
 }
 
 // ------------------------------------------------------ forest reuse
@@ -1099,14 +1112,15 @@ __global__ void k_reuse(View v) { reuse_body(v, blockIdx.x, gridDim.x); }
 struct ClusterSmem {
     int home_root[kClusterThreads / 32][32];
     float4 home_pt[kClusterThreads / 32][32];
-    int rstart[kClusterThreads / 32][9], rpre[kClusterThreads / 32][10];
+    int rstart[kClusterThreads / 32][kMaxRows], rpre[kClusterThreads / 32][kMaxRows + 1];
 };
 
-template <int MODE, int DIM>
+template <int MODE, int DK>
 __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
+    constexpr int DIM = DK & 3, K = (DK >> 2) + 1;  // dimension, cells per Eps
     float4(&home_pt)[kClusterThreads / 32][32] = sm.home_pt;
-    int(&rstart)[kClusterThreads / 32][9] = sm.rstart;
-    int(&rpre)[kClusterThreads / 32][10] = sm.rpre;
+    int(&rstart)[kClusterThreads / 32][kMaxRows] = sm.rstart;
+    int(&rpre)[kClusterThreads / 32][kMaxRows + 1] = sm.rpre;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     volatile int* rh = sm.home_root[wib];
     const float4* hpt = home_pt[wib];
@@ -1159,8 +1173,8 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
         const bool uni = __all_sync(kFull, !hcore || hh == r0);
         const int hmin = start + __ffs(hmask) - 1;
         int rs, re;
-        row_ranges<DIM, true>(v, T, gen, skey[start], lane, rs, re);
-        const int total = candidate_stream<Stencil<DIM, true>::kRows>(rs, re, hmin + 1, lane, rstart[wib], rpre[wib]);
+        row_ranges<DIM, true, K>(v, T, gen, skey[start], lane, rs, re);
+        const int total = candidate_stream<Stencil<DIM, true, K>::kRows>(rs, re, hmin + 1, lane, rstart[wib], rpre[wib]);
         int r = 0;
         for (int base = 0; base < total; base += 32) {
             const int idx = base + lane;
@@ -1204,10 +1218,10 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
     flush_stats(v, tally, err, lane);
 }
 
-template <int MODE, int DIM>
+template <int MODE, int DK>
 __global__ void __launch_bounds__(kClusterThreads, 8) k_union(View v) {
     __shared__ ClusterSmem sm;
-    union_body<MODE, DIM>(v, sm);
+    union_body<MODE, DK>(v, sm);
 }
 
 // Root of every core point, walked from the position's root hint.  Without
@@ -1217,8 +1231,9 @@ __global__ void __launch_bounds__(kClusterThreads, 8) k_union(View v) {
 // this slide) gets its list rebuilt here from one scan of the final grid --
 // each block queues such points of its 256-position tile in shared memory
 // and rebuilds them warp by warp.
-template <int MODE, int DIM>
+template <int MODE, int DK>
 __device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx, StreamSmem& sm) {
+    constexpr int DIM = DK & 3, K = (DK >> 2) + 1;  // dimension, cells per Eps
     if (bx == 0 && threadIdx.x == 0) v.ctl->label_next = 0;  // k_label's queue; not read here
     const long long b = v.ctl->b;
     const int cur = (int)(b & 1);
@@ -1229,8 +1244,8 @@ __device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx, Str
             v.sroot[i] = scnt[i] >= v.min_pts ? uf_find(v.parent, v.sroot[i]) : -1;
         return;
     }
-    int(&rstart)[8][9] = sm.rstart;
-    int(&rpre)[8][10] = sm.rpre;
+    int(&rstart)[8][kMaxRows] = sm.rstart;
+    int(&rpre)[8][kMaxRows + 1] = sm.rpre;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
     const unsigned gen = gen_of_build(b);
     const float4* spt = v.spt[cur];
@@ -1258,8 +1273,8 @@ __device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx, Str
             const float4 ap = spt[at];
             const int a = slot_of(ap);
             int rs, re;
-            row_ranges<DIM, false>(v, v.table[cur], gen, v.skey[cur][at], lane, rs, re);
-            const int total = candidate_stream<Stencil<DIM, false>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
+            row_ranges<DIM, false, K>(v, v.table[cur], gen, v.skey[cur][at], lane, rs, re);
+            const int total = candidate_stream<Stencil<DIM, false, K>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
             int r = 0, nfound = 0;
             for (int base = 0; base < total; base += 32) {
                 const int idx = base + lane;
@@ -1278,18 +1293,19 @@ __device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx, Str
     flush_stats(v, tally, 0, lane);
 }
 
-template <int MODE, int DIM>
+template <int MODE, int DK>
 __global__ void __launch_bounds__(256) k_flatten(View v) {
     __shared__ StreamSmem sm;
-    flatten_body<MODE, DIM>(v, blockIdx.x, gridDim.x, sm);
+    flatten_body<MODE, DK>(v, blockIdx.x, gridDim.x, sm);
 }
 
 // Labels and ids by slot: core -> 0 and its root; non-core -> 1 and the
 // minimum root over adjacent cores, or 2 and its own slot.
-template <int MODE, int DIM>
+template <int MODE, int DK>
 __device__ __forceinline__ void label_body(const View& v, int advance, int bx, ClusterSmem& sm) {
-    int(&rstart)[kClusterThreads / 32][9] = sm.rstart;
-    int(&rpre)[kClusterThreads / 32][10] = sm.rpre;
+    constexpr int DIM = DK & 3, K = (DK >> 2) + 1;  // dimension, cells per Eps
+    int(&rstart)[kClusterThreads / 32][kMaxRows] = sm.rstart;
+    int(&rpre)[kClusterThreads / 32][kMaxRows + 1] = sm.rpre;
     float4(&home_pt)[kClusterThreads / 32][32] = sm.home_pt;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const float4* hpt = home_pt[wib];
@@ -1336,8 +1352,8 @@ __device__ __forceinline__ void label_body(const View& v, int advance, int bx, C
         __syncwarp();
         home_pt[wib][lane] = h;
         int rs, re;
-        row_ranges<DIM, false>(v, T, gen, skey[start], lane, rs, re);
-        const int total = candidate_stream<Stencil<DIM, false>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
+        row_ranges<DIM, false, K>(v, T, gen, skey[start], lane, rs, re);
+        const int total = candidate_stream<Stencil<DIM, false, K>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
         int best = INT_MAX, r = 0;
         for (int base = 0; base < total; base += 32) {
             const int idx = base + lane;
@@ -1375,10 +1391,10 @@ __device__ __forceinline__ void label_body(const View& v, int advance, int bx, C
     }
 }
 
-template <int MODE, int DIM>
+template <int MODE, int DK>
 __global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advance) {
     __shared__ ClusterSmem sm;
-    label_body<MODE, DIM>(v, advance, blockIdx.x, sm);
+    label_body<MODE, DK>(v, advance, blockIdx.x, sm);
 }
 
 // Outputs by slot from the roots and the lists: core -> 0 and its root; a
@@ -1461,7 +1477,7 @@ template <> struct PhaseShape<kBatchLabel> { static constexpr int threads = kClu
 // instantiated per (MODE, DIM) and launched once per group of streams that
 // share them, so each instantiation holds one body (registers as in the
 // single-stream kernels); the other phases use MODE = DIM = 0.
-template <int PHASE, int MODE, int DIM>
+template <int PHASE, int MODE, int DK>
 __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>::min_blocks)
     k_batch(BatchLaunch L) {
     __shared__ View sv;
@@ -1500,7 +1516,7 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
         runmerge_body(sv, it.c, 0, bx % nruns, bx / nruns, words);
     } else if constexpr (PHASE == kBatchDecrement) {
         __shared__ StreamSmem sm;
-        decr_body<MODE, DIM>(sv, it.j, it.c, bx, sm);
+        decr_body<MODE, DK>(sv, it.j, it.c, bx, sm);
     } else if constexpr (PHASE == kBatchMerge) {
         __shared__ MergeSmem sm;
         merge_body(sv, it.j, it.c, 0, bx, nbx, sm);
@@ -1509,23 +1525,23 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
         build_body(sv, bx, sm);
     } else if constexpr (PHASE == kBatchIncrement) {
         __shared__ StreamSmem sm;
-        incr_body<MODE, DIM>(sv, it.j, it.c, 0, bx, sm);
+        incr_body<MODE, DK>(sv, it.j, it.c, 0, bx, sm);
     } else if constexpr (PHASE == kBatchDamage) {
         if (sv.list_cap >= 0) damage_body(sv, bx, nbx);
     } else if constexpr (PHASE == kBatchReuse) {
         if (sv.list_cap >= 0) reuse_body(sv, bx, nbx);
     } else if constexpr (PHASE == kBatchUnion) {
         __shared__ ClusterSmem sm;
-        union_body<MODE, DIM>(sv, sm);
+        union_body<MODE, DK>(sv, sm);
     } else if constexpr (PHASE == kBatchFlatten) {
         __shared__ StreamSmem sm;
-        flatten_body<MODE, DIM>(sv, bx, nbx, sm);
+        flatten_body<MODE, DK>(sv, bx, nbx, sm);
     } else {
         __shared__ ClusterSmem sm;
         if (sv.list_cap >= 0)
             border_body(sv, 1, bx, nbx);
         else
-            label_body<MODE, DIM>(sv, 1, bx, sm);
+            label_body<MODE, DK>(sv, 1, bx, sm);
     }
 }
 
@@ -1547,19 +1563,30 @@ void ensure_runmerge_smem() {
 
 }  // namespace
 
-#define RTDBS_DISPATCH(prec, dim, KERNEL, GRID, BLOCK, STREAM, ...)           \
+// Launch of a work kernel instantiated for (precision, DK); dk = dim + 4 (K - 1).
+#define RTDBS_DISPATCH(prec, dk_expr, KERNEL, GRID, BLOCK, STREAM, ...)          \
     do {                                                                         \
+        const int dk = (dk_expr);                                                \
         if ((prec) == kPrecFp32) {                                               \
-            if ((dim) == 1) KERNEL<kPrecFp32, 1><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);      \
-            else if ((dim) == 2) KERNEL<kPrecFp32, 2><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); \
-            else KERNEL<kPrecFp32, 3><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);                 \
+            switch (dk) {                                                        \
+                case 1: KERNEL<kPrecFp32, 1><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break; \
+                case 2: KERNEL<kPrecFp32, 2><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break; \
+                case 3: KERNEL<kPrecFp32, 3><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break; \
+                case 5: KERNEL<kPrecFp32, 5><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break; \
+                case 6: KERNEL<kPrecFp32, 6><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break; \
+                default: KERNEL<kPrecFp32, 7><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break; \
+            }                                                                    \
         } else {                                                                 \
-            if ((dim) == 1) KERNEL<kPrecFp64, 1><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);      \
-            else if ((dim) == 2) KERNEL<kPrecFp64, 2><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); \
-            else KERNEL<kPrecFp64, 3><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);                 \
+            switch (dk) {                                                        \
+                case 1: KERNEL<kPrecFp64, 1><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break; \
+                case 2: KERNEL<kPrecFp64, 2><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break; \
+                case 3: KERNEL<kPrecFp64, 3><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break; \
+                case 5: KERNEL<kPrecFp64, 5><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break; \
+                case 6: KERNEL<kPrecFp64, 6><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break; \
+                default: KERNEL<kPrecFp64, 7><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break; \
+            }                                                                    \
         }                                                                        \
     } while (0)
-
 
 cudaError_t configure_kernels() {
     int dev = 0;
@@ -1572,7 +1599,7 @@ cudaError_t configure_kernels() {
 
 cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, int init,
                          int stg_off, int advance, cudaStream_t s) {
-    const int warp_blocks = (c * kQueryLanes + 255) / 256;  // count passes: kQueryLanes per point
+    const int warp_blocks = (c * query_lanes(v.cell_mult) + 255) / 256;  // count passes
     switch (phase) {
         case kPhaseIngest:
             k_ingest<<<(c + 255) / 256, 256, 0, s>>>(v, j, c, init, stg_off);
@@ -1584,7 +1611,7 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
                          sizeof(unsigned long long) * c, s>>>(v, c, init);
             break;
         case kPhaseDecrement:
-            if (!init) RTDBS_DISPATCH(precision, v.dim, k_decr, warp_blocks, 256, s, v, j, c);
+            if (!init) RTDBS_DISPATCH(precision, dk_of(v), k_decr, warp_blocks, 256, s, v, j, c);
             break;
         case kPhaseMerge:
             k_merge<<<(v.W + kMergeTile - 1) / kMergeTile, kMergeThreads, 0, s>>>(v, j, c, init);
@@ -1593,7 +1620,7 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
             k_build<<<(v.W + kBuildThreads - 1) / kBuildThreads, kBuildThreads, 0, s>>>(v);
             break;
         case kPhaseIncrement:
-            RTDBS_DISPATCH(precision, v.dim, k_incr, warp_blocks, 256, s, v, j, c, init);
+            RTDBS_DISPATCH(precision, dk_of(v), k_incr, warp_blocks, 256, s, v, j, c, init);
             break;
         case kPhaseLabel:
             if (v.list_cap >= 0) {
@@ -1614,14 +1641,14 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
             const int need = (v.max_items + per_block - 1) / per_block;  // one warp per item at most
             const int blocks = max(1, min(sms * 6, need));
             if (phase == kPhaseUnion)
-                RTDBS_DISPATCH(precision, v.dim, k_union, max(1, min(sms * 8, need)), kClusterThreads, s, v);
+                RTDBS_DISPATCH(precision, dk_of(v), k_union, max(1, min(sms * 8, need)), kClusterThreads, s, v);
             else
-                RTDBS_DISPATCH(precision, v.dim, k_label, blocks, kClusterThreads, s, v, advance);
+                RTDBS_DISPATCH(precision, dk_of(v), k_label, blocks, kClusterThreads, s, v, advance);
             break;
         }
         case kPhaseFlatten: {
             const int sms = g_num_sms > 0 ? g_num_sms : 152;
-            RTDBS_DISPATCH(precision, v.dim, k_flatten, sms * 8, 256, s, v);
+            RTDBS_DISPATCH(precision, dk_of(v), k_flatten, sms * 8, 256, s, v);
             break;
         }
         default:
@@ -1666,7 +1693,7 @@ int batch_blocks(int phase, const View& v, int c) {
         case kBatchSort:
         case kBatchRunmerge: return 2 * runs;
         case kBatchDecrement:
-        case kBatchIncrement: return (c * kQueryLanes + 255) / 256;
+        case kBatchIncrement: return (c * query_lanes(v.cell_mult) + 255) / 256;
         case kBatchMerge: return (v.W + kMergeTile - 1) / kMergeTile;
         case kBatchBuild: return (v.W + kBuildThreads - 1) / kBuildThreads;
         case kBatchDamage:
@@ -1687,14 +1714,25 @@ bool batch_phase_split(int phase) {
 
 #define RTDBS_BATCH_MD(PH, GRID, BLOCK, STREAM)                                      \
     do {                                                                           \
+        const int dk = dim;                                                        \
         if (prec == kPrecFp32) {                                                   \
-            if (dim == 1) k_batch<PH, kPrecFp32, 1><<<GRID, BLOCK, 0, STREAM>>>(L);  \
-            else if (dim == 2) k_batch<PH, kPrecFp32, 2><<<GRID, BLOCK, 0, STREAM>>>(L); \
-            else k_batch<PH, kPrecFp32, 3><<<GRID, BLOCK, 0, STREAM>>>(L);           \
+            switch (dk) {                                                          \
+                case 1: k_batch<PH, kPrecFp32, 1><<<GRID, BLOCK, 0, STREAM>>>(L); break; \
+                case 2: k_batch<PH, kPrecFp32, 2><<<GRID, BLOCK, 0, STREAM>>>(L); break; \
+                case 3: k_batch<PH, kPrecFp32, 3><<<GRID, BLOCK, 0, STREAM>>>(L); break; \
+                case 5: k_batch<PH, kPrecFp32, 5><<<GRID, BLOCK, 0, STREAM>>>(L); break; \
+                case 6: k_batch<PH, kPrecFp32, 6><<<GRID, BLOCK, 0, STREAM>>>(L); break; \
+                default: k_batch<PH, kPrecFp32, 7><<<GRID, BLOCK, 0, STREAM>>>(L); break; \
+            }                                                                      \
         } else {                                                                   \
-            if (dim == 1) k_batch<PH, kPrecFp64, 1><<<GRID, BLOCK, 0, STREAM>>>(L);  \
-            else if (dim == 2) k_batch<PH, kPrecFp64, 2><<<GRID, BLOCK, 0, STREAM>>>(L); \
-            else k_batch<PH, kPrecFp64, 3><<<GRID, BLOCK, 0, STREAM>>>(L);           \
+            switch (dk) {                                                          \
+                case 1: k_batch<PH, kPrecFp64, 1><<<GRID, BLOCK, 0, STREAM>>>(L); break; \
+                case 2: k_batch<PH, kPrecFp64, 2><<<GRID, BLOCK, 0, STREAM>>>(L); break; \
+                case 3: k_batch<PH, kPrecFp64, 3><<<GRID, BLOCK, 0, STREAM>>>(L); break; \
+                case 5: k_batch<PH, kPrecFp64, 5><<<GRID, BLOCK, 0, STREAM>>>(L); break; \
+                case 6: k_batch<PH, kPrecFp64, 6><<<GRID, BLOCK, 0, STREAM>>>(L); break; \
+                default: k_batch<PH, kPrecFp64, 7><<<GRID, BLOCK, 0, STREAM>>>(L); break; \
+            }                                                                      \
         }                                                                          \
     } while (0)
 

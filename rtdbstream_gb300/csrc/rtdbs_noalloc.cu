@@ -161,6 +161,7 @@ extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int
     View v;
     std::memset(&v, 0, sizeof(v));
     v.dim = dim;
+    v.cell_mult = 1;
     v.W = n;
     v.S = n;
     v.units = 1;

@@ -45,7 +45,7 @@ class Params(ctypes.Structure):
                 ("min_pts", ctypes.c_int32), ("eps", ctypes.c_double), ("precision", ctypes.c_int32),
                 ("has_bbox", ctypes.c_int32), ("bbox_min", ctypes.c_float * 3),
                 ("bbox_max", ctypes.c_float * 3), ("device", ctypes.c_int32),
-                ("flags", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
+                ("flags", ctypes.c_int32), ("cell_mult", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
 
 
 class Stats(ctypes.Structure):
@@ -161,21 +161,10 @@ class Engine:
 
     def __init__(self, dim: int, window_size: int, stride_size: int, radius: float, min_pts: int,
                  precision: str = "fp64", bbox: Optional[Tuple] = None, device: int = 0,
-                 use_graph: bool = True, stream: int = 0):
+                 use_graph: bool = True, stream: int = 0, cell_mult: int = 1):
         self._lib = load_library()
-        p = Params()
-        _check(self._lib.rtdbs_params_init(ctypes.byref(p)))
-        p.dim, p.window, p.stride = int(dim), int(window_size), int(stride_size)
-        p.min_pts, p.eps = int(min_pts), float(radius)
-        p.precision = {"fp64": PREC_FP64, "fp32": PREC_FP32}[precision]
-        p.device = int(device)
-        p.flags = 0 if use_graph else FLAG_NO_GRAPH
-        if bbox is not None:
-            lo, hi = bbox
-            p.has_bbox = 1
-            for a in range(int(dim)):
-                p.bbox_min[a] = float(lo[a])
-                p.bbox_max[a] = float(hi[a])
+        p = make_params(dim, window_size, stride_size, radius, min_pts, precision=precision, bbox=bbox,
+                        device=device, use_graph=use_graph, cell_mult=cell_mult)
         self.params = p
         self.dim, self.window_size, self.stride_size = p.dim, p.window, p.stride
         self.radius, self.min_pts = p.eps, p.min_pts
@@ -267,7 +256,8 @@ class Engine:
 
 def make_params(dim: int, window_size: int, stride_size: int, radius: float, min_pts: int,
                 precision: str = "fp64", bbox: Optional[Tuple] = None, device: int = 0,
-                use_graph: bool = True) -> Params:
+                use_graph: bool = True, cell_mult: int = 1) -> Params:
+    """rtdbs_params for one stream; cell_mult = grid cells per Eps (1 or 2)."""
     L = load_library()
     p = Params()
     _check(L.rtdbs_params_init(ctypes.byref(p)))
@@ -276,6 +266,7 @@ def make_params(dim: int, window_size: int, stride_size: int, radius: float, min
     p.precision = {"fp64": PREC_FP64, "fp32": PREC_FP32}[precision]
     p.device = int(device)
     p.flags = 0 if use_graph else FLAG_NO_GRAPH
+    p.cell_mult = int(cell_mult)
     if bbox is not None:
         lo, hi = bbox
         p.has_bbox = 1

@@ -27,8 +27,9 @@ def _built():
         pytest.skip("no GPU")
 
 
-def run_stream(points, W, S, eps, mp, n_slides, precision="fp64", use_graph=True, bbox=None):
-    eng = Engine(points.shape[1], W, S, eps, mp, precision=precision, use_graph=use_graph, bbox=bbox)
+def run_stream(points, W, S, eps, mp, n_slides, precision="fp64", use_graph=True, bbox=None, cell_mult=1):
+    eng = Engine(points.shape[1], W, S, eps, mp, precision=precision, use_graph=use_graph, bbox=bbox,
+                 cell_mult=cell_mult)
     eng.load_window(points[:W])
     labs, cids, nns = [], [], []
     for k in range(n_slides):
@@ -260,3 +261,20 @@ def test_forest_reuse_matches_oracle(precision):
     a = np.argmin(((win - (0.0, 0.0)) ** 2).sum(1) + np.where(core, 0.0, 1e9))
     b = np.argmin(((win - (10.0, 0.0)) ** 2).sum(1) + np.where(core, 0.0, 1e9))
     assert cid[a] != cid[b]
+
+
+# Two grid cells per Eps: a (2K+1)^d = 5^d stencil of Eps/2 cells.  Same
+# labels, ids and counts as the oracle on every case shape: 1-D, 2-D, 3-D,
+# S = W, multi-chunk slides, FP32-band pairs, MinPts above the list cap.
+K2_CASES = [c for c in CASES if c[0] in ("mix2d_W10k_S1k", "walk3d_W60k_S6k", "band3d_W20k_S2k", "stk1d_W8k_S2k",
+                                          "big_stride_W40k_S20k", "S_eq_W_3d", "mix2d_mp40_W8k")]
+
+
+@pytest.mark.parametrize("name,gen,W,S,eps,mp,slides", K2_CASES, ids=[c[0] for c in K2_CASES])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_two_cells_per_eps_match_oracle(name, gen, W, S, eps, mp, slides, precision):
+    pts = gen()
+    got = run_stream(pts, W, S, eps, mp, slides, precision=precision, cell_mult=2)
+    mode = O.MODE_FP64 if precision == "fp64" else O.MODE_FP32
+    exp = O.stream(pts, W, S, eps, mp, mode, first_slide=1, n_out=slides)
+    assert_same(got[:3], exp, f"{name}/{precision}/K2")

@@ -151,3 +151,34 @@ def test_pool_rejects_unloaded_and_duplicate_streams():
         with pytest.raises(RtdbsError) as ei:
             pool.slide([sid, sid], d)
         assert ei.value.status == E.RTDBS_ERR_INVALID
+
+
+def test_pool_mixes_cell_multipliers():
+    """Streams with one and two cells per Eps in one pool (separate launch
+    groups) equal the same streams alone and the oracle."""
+    specs = [(2, 4_000, 400, 0.5, 5, 1), (2, 4_000, 400, 0.5, 5, 2), (3, 6_000, 600, 0.8, 6, 2),
+             (3, 6_000, 600, 0.8, 6, 1)]
+    data = [wl.gaussian_mixture(W + ROUNDS * S, dim=dim, k=6, box=20.0, seed=300 + i)
+            for i, (dim, W, S, eps, mp, km) in enumerate(specs)]
+    import torch
+
+    with Pool() as pool:
+        ids = []
+        for (dim, W, S, eps, mp, km), d in zip(specs, data):
+            sid = pool.add_stream(make_params(dim, W, S, eps, mp, cell_mult=km))
+            pool.load_window(sid, d[:W])
+            ids.append(sid)
+        for k in range(ROUNDS):
+            buf = torch.from_numpy(np.concatenate([d[W + k * S: W + (k + 1) * S].reshape(-1)
+                                                   for (dim, W, S, eps, mp, km), d in zip(specs, data)])).cuda()
+            pool.slide(ids, buf)
+        for sid, (dim, W, S, eps, mp, km), d in zip(ids, specs, data):
+            lab, cid = pool.outputs(sid)
+            with Engine(dim, W, S, eps, mp, cell_mult=km) as eng:
+                eng.load_window(d[:W])
+                for k in range(ROUNDS):
+                    elab, ecid = eng.slide(d[W + k * S: W + (k + 1) * S])
+            assert np.array_equal(lab, elab) and np.array_equal(cid, ecid)
+            win = O.window_of(d, W, S, ROUNDS)
+            _, olab, ocid, _ = O.window_grid(win, eps, mp, O.MODE_FP64)
+            assert np.array_equal(lab, olab) and np.array_equal(cid, ocid)
