@@ -413,13 +413,21 @@ def run_batched(args, dev, stream, flush, n_streams=256, rounds=None, plain_roun
     streams = wl.mixed_streams(n_streams)
     rounds = rounds or (args.warmup + max(10, args.steps // 5))
     data = [wl.mix_points(st, st.window + rounds * st.stride) for st in streams]
+    # launch configuration (cells per Eps, work split) per stream bucket, picked
+    # by the autotuner on each bucket's first stream; pool and plain engines use it
+    from rtdbstream_gb300.autotune import Autotuner
+
+    tuner = Autotuner(cache_path=os.path.join(ROOT, "_build", "autotune_batched.json"), device=dev)
+    tuned = [tuner.choose(d, st.dim, st.window, st.stride, st.eps, st.min_pts) for st, d in zip(streams, data)]
     packed = [torch.from_numpy(np.concatenate([d[st.window + k * st.stride: st.window + (k + 1) * st.stride]
                                                .reshape(-1) for st, d in zip(streams, data)])).to(dev)
               for k in range(rounds)]
     pool = Pool(device=dev, use_graph=True, stream=stream.cuda_stream)
     ids = []
     for st, d in zip(streams, data):
-        sid = pool.add_stream(make_params(st.dim, st.window, st.stride, st.eps, st.min_pts, device=dev))
+        c = tuned[len(ids)]
+        sid = pool.add_stream(make_params(st.dim, st.window, st.stride, st.eps, st.min_pts, device=dev,
+                                          cell_mult=c["cell_mult"], work_grab=c["work_grab"]))
         pool.load_window(sid, d[:st.window])
         ids.append(sid)
     for k in range(args.warmup):
@@ -457,7 +465,9 @@ def run_batched(args, dev, stream, flush, n_streams=256, rounds=None, plain_roun
     plain_ms = []
     engines = []
     for st, d in zip(streams, data):
-        e = Engine(st.dim, st.window, st.stride, st.eps, st.min_pts, device=dev, stream=stream.cuda_stream)
+        c = tuned[len(engines)]
+        e = Engine(st.dim, st.window, st.stride, st.eps, st.min_pts, device=dev, stream=stream.cuda_stream,
+                   cell_mult=c["cell_mult"], work_grab=c["work_grab"])
         e.load_window(d[:st.window])
         engines.append(e)
     offsets, o = [], 0
@@ -487,6 +497,8 @@ def run_batched(args, dev, stream, flush, n_streams=256, rounds=None, plain_roun
         "launches_per_round": stats["launches_per_round"], "graph_replays": stats["graph_replays"],
         "phase_ms": prof,
         "exact_sample_vs_fp64_oracle": exact,
+        "autotune": {"buckets": len(tuner.cache), "tuned_now": tuner.tuned, "tune_s": round(tuner.tune_seconds, 2),
+                     "choices": {k: [v["cell_mult"], v["work_grab"]] for k, v in sorted(tuner.cache.items())}},
     }
 
 

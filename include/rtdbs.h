@@ -92,7 +92,10 @@ typedef struct rtdbs_params {
                              work items where they are sparse (rtdbstream_gb300/autotune.py
                              picks it per stream).  The reference's grid has side Eps/sqrt(3)
                              (src/dbscan/dbscan.cpp:34-37) */
-    int32_t reserved[5];
+    int32_t work_grab;    /* work items (cell runs) a clustering warp takes from the shared
+                             queue at a time, 1..64 (0 = 8): the work split between warps,
+                             picked by rtdbstream_gb300/autotune.py.  No reference counterpart */
+    int32_t reserved[4];
 } rtdbs_params;
 
 /* Cumulative counters (src/dbscan/dbscan.cpp:145-212 keeps similar debug counters). */

@@ -2,7 +2,8 @@
 
 The numeric work runs in librtdbs.so (hand-written sm_103a CUDA kernels behind
 the C ABI of include/rtdbs.h).  This package holds the ctypes binding, the
-nvcc build step and seeded workload generators.
+nvcc build step, the launch-configuration autotuner and seeded workload
+generators.
 """
 from .engine import (PREC_FP32, PREC_FP64, Engine, Pool, RtdbsError, load_library,  # noqa: F401
                      make_params, stream_bytes)

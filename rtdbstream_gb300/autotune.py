@@ -1,0 +1,142 @@
+"""Autotuner for a stream's launch configuration.
+
+Two knobs change how the engine works without changing its results:
+- ``cell_mult`` (K): grid cells per Eps along each axis.  K = 2 scans the
+  (2K+1)^d = 5^d cells of side Eps/2 around a point, which tests fewer pairs
+  where cells are dense, but costs more cells, table lookups and work items
+  where they are sparse.
+- ``work_grab``: work items (cell runs) a clustering warp takes from the
+  shared queue at a time -- the work split between warps.  Small grabs balance
+  uneven items; large ones keep consecutive cells on one warp and cost fewer
+  queue atomics.
+
+Streams are grouped into buckets by dimension, predicate, window size and
+density (mean points per occupied Eps-cell of a sample window).  For a
+bucket seen for the first time the tuner times every candidate on an engine
+fed with that stream's own points (its first window, then a few slides,
+CUDA events around the slides), keeps the fastest and stores the choice in a
+JSON cache, so later streams of the bucket, and later runs, reuse it.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+import time
+from typing import Callable, Dict, Iterable, Optional, Tuple
+
+import numpy as np
+
+from .engine import Engine, make_params
+
+# (cell_mult, work_grab)
+CANDIDATES: Tuple[Tuple[int, int], ...] = ((1, 8), (1, 4), (1, 16), (2, 8), (2, 4), (2, 16))
+
+DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
+
+
+def density(points: np.ndarray, eps: float, sample: int = 200_000) -> float:
+    """Mean number of points per occupied cell of side Eps (a sample of at
+    most `sample` points, so large windows cost little)."""
+    pts = np.asarray(points, dtype=np.float64)
+    if len(pts) > sample:
+        pts = pts[:sample]
+    cells = np.floor((pts - pts.min(axis=0)) / eps).astype(np.int64)
+    _, counts = np.unique(cells, axis=0, return_counts=True)
+    return float(len(pts) / max(1, len(counts)))
+
+
+def bucket_key(dim: int, window: int, precision: str, dens: float) -> str:
+    """Buckets: powers of two of the window and of the density."""
+    wb = int(round(math.log2(max(window, 1))))
+    db = int(round(math.log2(max(dens, 1e-3))))
+    return f"d{dim}-{precision}-W2^{wb}-n2^{db}"
+
+
+class Autotuner:
+    """Picks (cell_mult, work_grab) per stream bucket.
+
+    `timer(points, dim, W, S, eps, min_pts, precision, cell_mult, work_grab)`
+    returns milliseconds per slide; the default times real slides on the GPU.
+    """
+
+    def __init__(self, cache_path: Optional[str] = None, device: int = 0, slides: int = 4,
+                 candidates: Iterable[Tuple[int, int]] = CANDIDATES, timer: Optional[Callable] = None):
+        self.cache_path = cache_path or os.environ.get("RTDBS_AUTOTUNE_CACHE") or DEFAULT_CACHE
+        self.device = device
+        self.slides = slides
+        self.candidates = tuple(candidates)
+        self.timer = timer or self._time_on_gpu
+        self.cache: Dict[str, dict] = {}
+        self.tuned = 0           # buckets timed in this process
+        self.tune_seconds = 0.0
+        if os.path.exists(self.cache_path):
+            try:
+                with open(self.cache_path) as f:
+                    self.cache = json.load(f)
+            except (OSError, ValueError):
+                self.cache = {}
+
+    def choose(self, points: np.ndarray, dim: int, window: int, stride: int, eps: float, min_pts: int,
+               precision: str = "fp64") -> dict:
+        """The bucket's configuration: {"cell_mult", "work_grab", "ms"}."""
+        key = bucket_key(dim, window, precision, density(points[:window], eps))
+        hit = self.cache.get(key)
+        if hit is not None:
+            return hit
+        t0 = time.perf_counter()
+        ms = {}
+        for km, grab in self.candidates:
+            try:
+                ms[f"{km},{grab}"] = float(self.timer(points, dim, window, stride, eps, min_pts, precision,
+                                                      km, grab))
+            except Exception:  # a configuration the stream cannot take is skipped
+                continue
+        if not ms:
+            raise RuntimeError(f"autotune: no candidate configuration ran for bucket {key}")
+        best = min(ms, key=ms.get)
+        km, grab = (int(x) for x in best.split(","))
+        self.cache[key] = {"cell_mult": km, "work_grab": grab, "ms": ms}
+        self.tuned += 1
+        self.tune_seconds += time.perf_counter() - t0
+        self._save()
+        return self.cache[key]
+
+    def params(self, points: np.ndarray, dim: int, window: int, stride: int, eps: float, min_pts: int,
+               precision: str = "fp64", **kw):
+        """rtdbs_params of a stream with the tuned configuration."""
+        c = self.choose(points, dim, window, stride, eps, min_pts, precision)
+        return make_params(dim, window, stride, eps, min_pts, precision=precision,
+                           cell_mult=c["cell_mult"], work_grab=c["work_grab"], **kw)
+
+    def _save(self) -> None:
+        d = os.path.dirname(self.cache_path)
+        if d:
+            os.makedirs(d, exist_ok=True)
+        tmp = self.cache_path + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(self.cache, f, indent=1, sort_keys=True)
+        os.replace(tmp, self.cache_path)
+
+    def _time_on_gpu(self, points, dim, window, stride, eps, min_pts, precision, cell_mult, work_grab):
+        import torch
+
+        need = window + (self.slides + 1) * stride
+        if len(points) < need:
+            raise ValueError("autotune: the sample needs a window and a few strides of points")
+        dev = torch.device("cuda", self.device)
+        s = torch.cuda.Stream(device=dev)
+        d = torch.from_numpy(np.ascontiguousarray(points[window:need], dtype=np.float32)).to(dev)
+        torch.cuda.synchronize(dev)  # the copy is on torch's stream, the slides on s
+        with torch.cuda.stream(s):
+            with Engine(dim, window, stride, eps, min_pts, precision=precision, device=self.device,
+                        stream=s.cuda_stream, cell_mult=cell_mult, work_grab=work_grab) as eng:
+                eng.load_window(points[:window])
+                eng.slide_async(d[:stride])   # warm-up (and the graph capture)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(s)
+                for k in range(1, self.slides + 1):
+                    eng.slide_async(d[k * stride:(k + 1) * stride])
+                b.record(s)
+                eng.sync()
+                return a.elapsed_time(b) / self.slides

@@ -359,6 +359,8 @@ int rtdbs_create(const rtdbs_params* params, void* cuda_stream, rtdbs_engine** o
         return fail(RTDBS_ERR_INVALID, "unknown precision mode %d", p.precision);
     if (p.cell_mult < 0 || p.cell_mult > 2)
         return fail(RTDBS_ERR_INVALID, "cell_mult must be 0 (default), 1 or 2 (got %d)", p.cell_mult);
+    if (p.work_grab < 0 || p.work_grab > 64)
+        return fail(RTDBS_ERR_INVALID, "work_grab must be 0 (default) or 1..64 (got %d)", p.work_grab);
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(RTDBS_ERR_NO_DEVICE, "no CUDA device available");
@@ -384,6 +386,7 @@ int rtdbs_create(const rtdbs_params* params, void* cuda_stream, rtdbs_engine** o
     View& v = e->v;
     v.dim = p.dim;
     v.cell_mult = p.cell_mult > 0 ? p.cell_mult : 1;
+    v.grab = p.work_grab > 0 ? p.work_grab : rtdbs::kBatch;
     v.W = p.window;
     v.S = p.stride;
     v.min_pts = p.min_pts;

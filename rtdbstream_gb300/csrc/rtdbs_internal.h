@@ -42,7 +42,7 @@ constexpr int kMergeThreads = 256;
 constexpr int kSortRun = 1024;     // words per radix-sort CTA (one per thread)
 constexpr int kBuildThreads = 512;
 constexpr int kClusterThreads = 256;
-constexpr int kBatch = 8;          // work items a clustering warp takes at a time
+constexpr int kBatch = 8;          // default work items a clustering warp takes at a time
 constexpr int kMaxIter = 1 << 20;  // bound on every device-side retry loop
 constexpr int kListCap = 30;       // longest neighbour list kept (MinPts <= 32)
 
@@ -85,6 +85,7 @@ struct View {
     int shift[3];
     int dim;
     int cell_mult;              // K: cells per Eps along each axis (1 or 2)
+    int grab;                   // work items a clustering warp takes from the queue at a time
     // parameters
     int W, S, min_pts, units;   // units = W / S
     int chunk;                  // C

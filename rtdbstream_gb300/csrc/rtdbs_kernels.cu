@@ -1139,17 +1139,17 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
     volatile int* hint = v.sroot;
     Tally tally;
     int err = 0;
-    // Warps take batches of kBatch consecutive work items (neighbouring
+    // Warps take batches of v.grab consecutive work items (neighbouring
     // cells: candidate loads reuse L1) from a counter, so uneven items do not
     // leave warps idle at the end.
     int it1 = 0;
     for (int itx = nitems;;) {
         if (itx >= it1) {
             int got = 0;
-            if (lane == 0) got = atomicAdd(&v.ctl->union_next, kBatch);
+            if (lane == 0) got = atomicAdd(&v.ctl->union_next, v.grab);
             itx = __shfl_sync(kFull, got, 0);
             if (itx >= nitems) break;
-            it1 = min(itx + kBatch, nitems);
+            it1 = min(itx + v.grab, nitems);
         }
         const int2 item = v.items[itx++];
         const int start = item.x, len = item.y;
@@ -1322,10 +1322,10 @@ __device__ __forceinline__ void label_body(const View& v, int advance, int bx, C
     for (int itx = nitems;;) {
         if (itx >= it1) {
             int got = 0;
-            if (lane == 0) got = atomicAdd(&v.ctl->label_next, kBatch);
+            if (lane == 0) got = atomicAdd(&v.ctl->label_next, v.grab);
             itx = __shfl_sync(kFull, got, 0);
             if (itx >= nitems) break;
-            it1 = min(itx + kBatch, nitems);
+            it1 = min(itx + v.grab, nitems);
         }
         const int2 item = v.items[itx++];
         const int start = item.x, len = item.y;

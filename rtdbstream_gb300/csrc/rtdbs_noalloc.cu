@@ -162,6 +162,7 @@ extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int
     std::memset(&v, 0, sizeof(v));
     v.dim = dim;
     v.cell_mult = 1;
+    v.grab = rtdbs::kBatch;
     v.W = n;
     v.S = n;
     v.units = 1;

@@ -55,7 +55,8 @@ def test_params_init_defaults(lib):
 
 @pytest.mark.parametrize("field,value", [("dim", 4), ("dim", 0), ("stride", 7), ("eps", 0.0),
                                          ("eps", float("nan")), ("precision", 9), ("stride", 0),
-                                         ("cell_mult", 3), ("cell_mult", -1)])
+                                         ("cell_mult", 3), ("cell_mult", -1), ("work_grab", 65),
+                                         ("work_grab", -2)])
 def test_invalid_params_rejected_before_device(lib, field, value):
     p = E.Params()
     lib.rtdbs_params_init(ctypes.byref(p))

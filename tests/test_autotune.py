@@ -1,0 +1,84 @@
+"""Autotuner: bucket choice, fastest-candidate selection and the JSON cache
+(CPU, with a stand-in timer); on the GPU, a tuned stream still matches the
+oracle exactly."""
+import json
+
+import numpy as np
+import pytest
+
+from rtdbstream_gb300 import autotune as AT
+from rtdbstream_gb300 import workloads as wl
+
+
+def fake_timer(table, calls):
+    def timer(points, dim, W, S, eps, mp, prec, km, grab):
+        calls.append((km, grab))
+        if (km, grab) not in table:
+            raise RuntimeError("configuration not available")
+        return table[(km, grab)]
+    return timer
+
+
+def test_density_and_buckets():
+    dense = wl.gaussian_mixture(20_000, dim=2, k=3, box=10.0, sigma=0.3, seed=1)
+    sparse = wl.gaussian_mixture(20_000, dim=2, k=3, box=1000.0, sigma=30.0, seed=1)
+    assert AT.density(dense, 0.5) > 10 * AT.density(sparse, 0.5)
+    assert AT.bucket_key(2, 20_000, "fp64", AT.density(dense, 0.5)) != \
+        AT.bucket_key(2, 20_000, "fp64", AT.density(sparse, 0.5))
+    assert AT.bucket_key(3, 1_000_000, "fp32", 3.6) == "d3-fp32-W2^20-n2^2"
+
+
+def test_picks_fastest_and_caches(tmp_path):
+    cache = tmp_path / "tune.json"
+    table = {(1, 8): 2.0, (1, 4): 1.5, (2, 8): 1.2, (2, 4): 3.0}   # (1, 16), (2, 16) unavailable
+    calls = []
+    tuner = AT.Autotuner(cache_path=str(cache), timer=fake_timer(table, calls))
+    pts = wl.gaussian_mixture(12_000, dim=2, k=4, box=20.0, seed=2)
+    c = tuner.choose(pts, 2, 10_000, 500, 0.5, 5)
+    assert (c["cell_mult"], c["work_grab"]) == (2, 8)
+    assert len(calls) == len(AT.CANDIDATES) and tuner.tuned == 1
+    # another stream of the same bucket: no timing
+    pts2 = wl.gaussian_mixture(12_000, dim=2, k=4, box=20.0, seed=3)
+    calls.clear()
+    assert tuner.choose(pts2, 2, 10_000, 500, 0.5, 5) == c and not calls
+    # the cache survives the process: a new tuner reads it
+    saved = json.loads(cache.read_text())
+    assert list(saved.values())[0]["cell_mult"] == 2
+    calls.clear()
+    again = AT.Autotuner(cache_path=str(cache), timer=fake_timer(table, calls))
+    assert again.choose(pts, 2, 10_000, 500, 0.5, 5)["work_grab"] == 8 and not calls
+
+
+def test_no_candidate_raises(tmp_path):
+    tuner = AT.Autotuner(cache_path=str(tmp_path / "t.json"), timer=fake_timer({}, []))
+    pts = wl.gaussian_mixture(3_000, dim=2, k=2, box=10.0, seed=4)
+    with pytest.raises(RuntimeError):
+        tuner.choose(pts, 2, 2_000, 200, 0.5, 5)
+
+
+@pytest.mark.gpu
+def test_tuned_streams_match_oracle(tmp_path):
+    import oracle as O
+
+    O.build(ref=False)
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    from rtdbstream_gb300 import Engine
+
+    tuner = AT.Autotuner(cache_path=str(tmp_path / "tune.json"), slides=3)
+    cases = [  # dense 2-D clusters, sparse 3-D walkers
+        (wl.gaussian_mixture(8_000 + 6 * 800, dim=2, k=3, box=10.0, sigma=0.3, seed=5), 2, 8_000, 800, 0.3, 8),
+        (wl.random_walkers(12_000 + 6 * 1_200, n_walkers=60, seed=6), 3, 12_000, 1_200, 3.3e-3, 10),
+    ]
+    for pts, dim, W, S, eps, mp in cases:
+        c = tuner.choose(pts, dim, W, S, eps, mp)
+        assert (c["cell_mult"], c["work_grab"]) in AT.CANDIDATES
+        assert len(c["ms"]) == len(AT.CANDIDATES) and all(v > 0 for v in c["ms"].values())
+        with Engine(dim, W, S, eps, mp, cell_mult=c["cell_mult"], work_grab=c["work_grab"]) as eng:
+            eng.load_window(pts[:W])
+            for k in range(2):
+                lab, cid = eng.slide(pts[W + k * S: W + (k + 1) * S])
+        win = O.window_of(pts, W, S, 2)
+        _, elab, ecid, _ = O.window_grid(win, eps, mp, O.MODE_FP64)
+        assert np.array_equal(lab, elab) and np.array_equal(cid, ecid)
