@@ -417,8 +417,11 @@ def run_batched(args, dev, stream, flush, n_streams=256, rounds=None, plain_roun
     # by the autotuner on each bucket's first stream; pool and plain engines use it
     from rtdbstream_gb300.autotune import Autotuner
 
+    # (pool rounds for the pool, single engines for the plain path: each at its best)
     tuner = Autotuner(cache_path=os.path.join(ROOT, "_build", "autotune_batched.json"), device=dev)
-    tuned = [tuner.choose(d, st.dim, st.window, st.stride, st.eps, st.min_pts) for st, d in zip(streams, data)]
+    tuned = tuner.choose_batched([(d, st.dim, st.window, st.stride, st.eps, st.min_pts, "fp64")
+                                  for st, d in zip(streams, data)])
+    tuned_plain = [tuner.choose(d, st.dim, st.window, st.stride, st.eps, st.min_pts) for st, d in zip(streams, data)]
     packed = [torch.from_numpy(np.concatenate([d[st.window + k * st.stride: st.window + (k + 1) * st.stride]
                                                .reshape(-1) for st, d in zip(streams, data)])).to(dev)
               for k in range(rounds)]
@@ -465,7 +468,7 @@ def run_batched(args, dev, stream, flush, n_streams=256, rounds=None, plain_roun
     plain_ms = []
     engines = []
     for st, d in zip(streams, data):
-        c = tuned[len(engines)]
+        c = tuned_plain[len(engines)]
         e = Engine(st.dim, st.window, st.stride, st.eps, st.min_pts, device=dev, stream=stream.cuda_stream,
                    cell_mult=c["cell_mult"], work_grab=c["work_grab"])
         e.load_window(d[:st.window])
@@ -498,7 +501,10 @@ def run_batched(args, dev, stream, flush, n_streams=256, rounds=None, plain_roun
         "phase_ms": prof,
         "exact_sample_vs_fp64_oracle": exact,
         "autotune": {"buckets": len(tuner.cache), "tuned_now": tuner.tuned, "tune_s": round(tuner.tune_seconds, 2),
-                     "choices": {k: [v["cell_mult"], v["work_grab"]] for k, v in sorted(tuner.cache.items())}},
+                     "choices": {k: [v["cell_mult"], v["work_grab"]] for k, v in sorted(tuner.cache.items())
+                                 if k.startswith("pool:")},
+                     "plain_choices": {k: [v["cell_mult"], v["work_grab"]] for k, v in sorted(tuner.cache.items())
+                                       if not k.startswith("pool:")}},
     }
 
 

@@ -12,10 +12,15 @@ Two knobs change how the engine works without changing its results:
 
 Streams are grouped into buckets by dimension, predicate, window size and
 density (mean points per occupied Eps-cell of a sample window).  For a
-bucket seen for the first time the tuner times every candidate on an engine
-fed with that stream's own points (its first window, then a few slides,
-CUDA events around the slides), keeps the fastest and stores the choice in a
-JSON cache, so later streams of the bucket, and later runs, reuse it.
+bucket seen for the first time the tuner times every candidate on the
+stream's own points and stores the choice in a JSON cache, so later streams
+of the bucket, and later runs, reuse it.  A stream slid alone is latency-bound
+and one slid in a pool round is throughput-bound, so the two are tuned
+apart: `choose` times a single engine (its first window, then a few slides),
+`choose_batched` times pool rounds over up to 16 streams of each bucket
+together.  The default (one cell per Eps, 8 items per grab) is kept unless a
+candidate is at least 3% faster, so timing noise does not pick a
+configuration.
 """
 from __future__ import annotations
 
@@ -29,8 +34,10 @@ import numpy as np
 
 from .engine import Engine, make_params
 
-# (cell_mult, work_grab)
+# (cell_mult, work_grab); the first is the default
 CANDIDATES: Tuple[Tuple[int, int], ...] = ((1, 8), (1, 4), (1, 16), (2, 8), (2, 4), (2, 16))
+MARGIN = 0.97           # a candidate replaces the default only when this much faster
+POOL_STREAMS = 16       # streams of a bucket timed together by choose_batched
 
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
 
@@ -61,12 +68,14 @@ class Autotuner:
     """
 
     def __init__(self, cache_path: Optional[str] = None, device: int = 0, slides: int = 4,
-                 candidates: Iterable[Tuple[int, int]] = CANDIDATES, timer: Optional[Callable] = None):
+                 candidates: Iterable[Tuple[int, int]] = CANDIDATES, timer: Optional[Callable] = None,
+                 pool_timer: Optional[Callable] = None):
         self.cache_path = cache_path or os.environ.get("RTDBS_AUTOTUNE_CACHE") or DEFAULT_CACHE
         self.device = device
         self.slides = slides
         self.candidates = tuple(candidates)
         self.timer = timer or self._time_on_gpu
+        self.pool_timer = pool_timer or self._time_pool_on_gpu
         self.cache: Dict[str, dict] = {}
         self.tuned = 0           # buckets timed in this process
         self.tune_seconds = 0.0
@@ -84,17 +93,38 @@ class Autotuner:
         hit = self.cache.get(key)
         if hit is not None:
             return hit
+        return self._tune(key, lambda km, grab: self.timer(points, dim, window, stride, eps, min_pts,
+                                                             precision, km, grab))
+
+    def choose_batched(self, streams) -> list:
+        """Configurations for streams slid together in pool rounds.  `streams`
+        holds (points, dim, window, stride, eps, min_pts, precision) tuples
+        (points: a window and a few strides); returns one configuration per
+        stream, tuned per bucket on pool rounds of the bucket's streams."""
+        keys = [("pool:" + bucket_key(st[1], st[2], st[6], density(st[0][:st[2]], st[4]))) for st in streams]
+        groups: Dict[str, list] = {}
+        for k, st in zip(keys, streams):
+            groups.setdefault(k, []).append(st)
+        for k, members in groups.items():
+            if k not in self.cache:
+                sel = members[:POOL_STREAMS]
+                self._tune(k, lambda km, grab: self.pool_timer(sel, km, grab))
+        return [self.cache[k] for k in keys]
+
+    def _tune(self, key: str, run: Callable) -> dict:
         t0 = time.perf_counter()
         ms = {}
         for km, grab in self.candidates:
             try:
-                ms[f"{km},{grab}"] = float(self.timer(points, dim, window, stride, eps, min_pts, precision,
-                                                      km, grab))
+                ms[f"{km},{grab}"] = float(run(km, grab))
             except Exception:  # a configuration the stream cannot take is skipped
                 continue
         if not ms:
             raise RuntimeError(f"autotune: no candidate configuration ran for bucket {key}")
         best = min(ms, key=ms.get)
+        default = "{},{}".format(*self.candidates[0])
+        if default in ms and ms[best] > MARGIN * ms[default]:
+            best = default
         km, grab = (int(x) for x in best.split(","))
         self.cache[key] = {"cell_mult": km, "work_grab": grab, "ms": ms}
         self.tuned += 1
@@ -140,3 +170,37 @@ class Autotuner:
                 b.record(s)
                 eng.sync()
                 return a.elapsed_time(b) / self.slides
+
+    def _time_pool_on_gpu(self, streams, cell_mult, work_grab, rounds: int = 3):
+        import torch
+
+        from .engine import Pool
+
+        dev = torch.device("cuda", self.device)
+        s = torch.cuda.Stream(device=dev)
+        need = rounds + 2
+        for pts, dim, W, S, eps, mp, prec in streams:
+            if len(pts) < W + need * S:
+                raise ValueError("autotune: the sample needs a window and a few strides of points")
+        packed = [torch.from_numpy(np.concatenate([np.ascontiguousarray(pts[W + k * S: W + (k + 1) * S],
+                                                                        dtype=np.float32).reshape(-1)
+                                                   for pts, dim, W, S, eps, mp, prec in streams])).to(dev)
+                  for k in range(need)]
+        torch.cuda.synchronize(dev)
+        with torch.cuda.stream(s):
+            with Pool(device=self.device, use_graph=True, stream=s.cuda_stream) as pool:
+                ids = []
+                for pts, dim, W, S, eps, mp, prec in streams:
+                    sid = pool.add_stream(make_params(dim, W, S, eps, mp, precision=prec, device=self.device,
+                                                      cell_mult=cell_mult, work_grab=work_grab))
+                    pool.load_window(sid, pts[:W])
+                    ids.append(sid)
+                pool.slide(ids, packed[0])
+                pool.slide(ids, packed[1])   # warm-up and the graph capture
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(s)
+                for k in range(2, need):
+                    pool.slide(ids, packed[k])
+                b.record(s)
+                pool.sync()
+                return a.elapsed_time(b) / rounds

@@ -82,3 +82,30 @@ def test_tuned_streams_match_oracle(tmp_path):
         win = O.window_of(pts, W, S, 2)
         _, elab, ecid, _ = O.window_grid(win, eps, mp, O.MODE_FP64)
         assert np.array_equal(lab, elab) and np.array_equal(cid, ecid)
+    # pool rounds: every candidate timed on the bucket's streams together
+    got = tuner.choose_batched([(pts, dim, W, S, eps, mp, "fp64") for pts, dim, W, S, eps, mp in cases])
+    for c in got:
+        assert (c["cell_mult"], c["work_grab"]) in AT.CANDIDATES and len(c["ms"]) == len(AT.CANDIDATES)
+
+
+def test_batched_tuning_per_bucket_and_margin(tmp_path):
+    calls = []
+
+    def pool_timer(streams, km, grab):
+        calls.append((len(streams), km, grab))
+        return {(1, 8): 1.0, (1, 4): 0.99, (2, 8): 0.5}.get((km, grab), 2.0)
+
+    tuner = AT.Autotuner(cache_path=str(tmp_path / "t.json"), timer=fake_timer({}, []), pool_timer=pool_timer)
+    dense = wl.gaussian_mixture(6_000, dim=2, k=2, box=5.0, sigma=0.2, seed=7)
+    sparse = wl.gaussian_mixture(6_000, dim=2, k=2, box=500.0, sigma=20.0, seed=8)
+    streams = [(dense, 2, 4_000, 400, 0.3, 5, "fp64")] * 20 + [(sparse, 2, 4_000, 400, 0.3, 5, "fp64")]
+    out = tuner.choose_batched(streams)
+    assert len(out) == 21
+    # two buckets, each timed once per candidate, at most 16 streams together
+    assert len(calls) == 2 * len(AT.CANDIDATES) and max(n for n, _, _ in calls) == AT.POOL_STREAMS
+    assert (out[0]["cell_mult"], out[0]["work_grab"]) == (2, 8)       # 2x faster: taken
+    # (1, 4) is only 1% faster than the default: the default is kept
+    tuner2 = AT.Autotuner(cache_path=str(tmp_path / "t2.json"), timer=fake_timer({}, []),
+                          pool_timer=lambda st, km, grab: {(1, 8): 1.0, (1, 4): 0.99}.get((km, grab), 2.0))
+    assert (tuner2.choose_batched(streams[:1])[0]["cell_mult"], tuner2.choose_batched(streams[:1])[0]["work_grab"]) \
+        == (1, 8)
