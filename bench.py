@@ -465,37 +465,47 @@ def run_batched(args, dev, stream, flush, n_streams=256, rounds=None, plain_roun
     pool.close()
 
     # the plain path: the same streams, one engine each, slid one at a time
-    plain_ms = []
-    engines = []
-    for st, d in zip(streams, data):
-        c = tuned_plain[len(engines)]
-        e = Engine(st.dim, st.window, st.stride, st.eps, st.min_pts, device=dev, stream=stream.cuda_stream,
-                   cell_mult=c["cell_mult"], work_grab=c["work_grab"])
-        e.load_window(d[:st.window])
-        engines.append(e)
+    # (with the autotuner's single-engine choices, and with the default
+    # configuration for reference)
     offsets, o = [], 0
     for st in streams:
         offsets.append(o)
         o += st.stride * st.dim
-    for k in range(min(plain_rounds, rounds)):
-        flush.fill_(float(k))
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        for e, st, off in zip(engines, streams, offsets):
-            e.slide_async(packed[k][off: off + st.stride * st.dim])
-        b.record(stream)
-        torch.cuda.synchronize()
-        if k > 0:
-            plain_ms.append(a.elapsed_time(b))
-    for e in engines:
-        e.close()
+
+    def plain_round_ms(configs):
+        engines = []
+        for st, d, c in zip(streams, data, configs):
+            e = Engine(st.dim, st.window, st.stride, st.eps, st.min_pts, device=dev, stream=stream.cuda_stream,
+                       cell_mult=c["cell_mult"], work_grab=c["work_grab"])
+            e.load_window(d[:st.window])
+            engines.append(e)
+        ms = []
+        for k in range(min(plain_rounds, rounds)):
+            flush.fill_(float(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for e, st, off in zip(engines, streams, offsets):
+                e.slide_async(packed[k][off: off + st.stride * st.dim])
+            b.record(stream)
+            torch.cuda.synchronize()
+            if k > 0:
+                ms.append(a.elapsed_time(b))
+        for e in engines:
+            e.close()
+        return statistics.mean(ms)
+
+    plain_ms = [plain_round_ms(tuned_plain)]
+    default_ms = plain_round_ms([{"cell_mult": 1, "work_grab": 8}] * len(streams))
     plain_value = slid / (statistics.mean(plain_ms) / 1000.0)
     return {
         "workload": f"{n_streams} streams, dim 2/3, W log-uniform 1k..200k (sum {sum(st.window for st in streams):,}),"
                     f" S 1-10% of W (sum {slid:,} per round), mixture data, Eps for 10-30 mean neighbours",
         "value": value, "unit": UNIT, "rounds": len(timed),
         "round_ms_p50": float(np.percentile(per_round, 50)), "round_ms_p99": float(np.percentile(per_round, 99)),
-        "plain_one_at_a_time": {"value": plain_value, "round_ms": statistics.mean(plain_ms)},
+        "plain_one_at_a_time": {"value": plain_value, "round_ms": statistics.mean(plain_ms),
+                                "config": "autotuned per stream bucket on single-engine slides"},
+        "plain_one_at_a_time_default": {"value": slid / (default_ms / 1000.0), "round_ms": default_ms,
+                                        "config": "1 cell per Eps, 8 items per grab"},
         "speedup_vs_plain": value / plain_value,
         "launches_per_round": stats["launches_per_round"], "graph_replays": stats["graph_replays"],
         "phase_ms": prof,
