@@ -10,7 +10,7 @@
 // Extra options: --fp64 (FP64 neighbour relation; default FP32, the
 // reference's), --warmup k (untimed passes over the stream first, the
 // reference does 10), --labels out.bin (label and cluster id of the last
-// window, int32 pairs by slot).
+// window, int32 pairs by slot), --cells-per-eps K (grid cells per Eps, 1 or 2).
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -33,7 +33,8 @@ void usage(const char* argv0) {
                  "         --radius | -R <float>    Eps\n"
                  "         --fp64                   FP64 neighbour relation (default: FP32)\n"
                  "         --warmup <int>           untimed passes first (default 0)\n"
-                 "         --labels <file>          write the last window's labels and ids\n",
+                 "         --labels <file>          write the last window's labels and ids\n"
+                 "         --cells-per-eps <1|2>    grid cells per Eps (default 1)\n",
                  argv0);
     std::exit(1);
 }
@@ -48,7 +49,7 @@ int die(const char* what, int rc) {
 int main(int argc, char** argv) {
     std::string file, labels_out;
     long long n = 0;
-    int W = 0, S = 0, K = 0, warmup = 0, precision = RTDBS_PREC_FP32;
+    int W = 0, S = 0, K = 0, warmup = 0, precision = RTDBS_PREC_FP32, cell_mult = 1;
     double R = 0.0;
     for (int i = 1; i < argc; ++i) {
         const std::string a(argv[i]);
@@ -66,6 +67,7 @@ int main(int argc, char** argv) {
         else if (a == "--fp64") precision = RTDBS_PREC_FP64;
         else if (a == "--warmup") warmup = std::atoi(next());
         else if (a == "--labels") labels_out = next();
+        else if (a == "--cells-per-eps") cell_mult = std::atoi(next());
         else {
             std::fprintf(stderr, "Unknown option '%s'\n", a.c_str());
             usage(argv[0]);
@@ -103,6 +105,7 @@ int main(int argc, char** argv) {
     p.min_pts = K;
     p.eps = R;
     p.precision = precision;
+    p.cell_mult = cell_mult;
     p.has_bbox = 1;
     for (int a = 0; a < 3; ++a) {
         p.bbox_min[a] = lo[a];

@@ -13,7 +13,8 @@ from rtdbstream_gb300 import workloads as wl
 pytestmark = pytest.mark.gpu
 
 
-def test_cli_tao_stream(tmp_path):
+@pytest.mark.parametrize("cells_per_eps", [1, 2])
+def test_cli_tao_stream(tmp_path, cells_per_eps):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no GPU")
@@ -25,7 +26,8 @@ def test_cli_tao_stream(tmp_path):
     out = tmp_path / "labels.bin"
     W, S, K, R = 1_000, 250, 5, 1.0
     r = subprocess.run([rbuild.CLI, "-f", str(path), "-n", "3000", "-W", str(W), "-S", str(S), "-K", str(K),
-                        "-R", str(R), "--labels", str(out)], capture_output=True, text=True, timeout=300)
+                        "-R", str(R), "--labels", str(out), "--cells-per-eps", str(cells_per_eps)],
+                       capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert "[Time] total:" in r.stdout
     slides = (3_000 - W) // S
