@@ -1648,7 +1648,7 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
         }
         case kPhaseFlatten: {
             const int sms = g_num_sms > 0 ? g_num_sms : 152;
-            RTDBS_DISPATCH(precision, dk_of(v), k_flatten, sms * 8, 256, s, v);
+            RTDBS_DISPATCH(precision, dk_of(v), k_flatten, sms * 16, 256, s, v);
             break;
         }
         default:

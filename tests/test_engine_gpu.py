@@ -278,3 +278,23 @@ def test_two_cells_per_eps_match_oracle(name, gen, W, S, eps, mp, slides, precis
     mode = O.MODE_FP64 if precision == "fp64" else O.MODE_FP32
     exp = O.stream(pts, W, S, eps, mp, mode, first_slide=1, n_out=slides)
     assert_same(got[:3], exp, f"{name}/{precision}/K2")
+
+
+# Edge shapes: one-point strides, tiny windows, MinPts 1 (every point core)
+# and 2 (empty neighbour lists), duplicates at one location, 1-D.
+EDGE_CASES = [
+    ("S1_W64_2d", lambda: wl.gaussian_mixture(64 + 40, dim=2, k=2, box=3.0, seed=41), 64, 1, 0.5, 4),
+    ("mp1_3d", lambda: wl.gaussian_mixture(2_000 + 3 * 200, dim=3, k=4, box=10.0, seed=42), 2_000, 200, 0.8, 1),
+    ("mp2_2d", lambda: wl.gaussian_mixture(2_000 + 3 * 200, dim=2, k=4, box=40.0, seed=43), 2_000, 200, 0.3, 2),
+    ("dups_1d", lambda: np.repeat(np.linspace(0, 5, 300, dtype=np.float32)[:, None], 4, axis=0), 800, 100, 0.02, 5),
+]
+
+
+@pytest.mark.parametrize("name,gen,W,S,eps,mp", EDGE_CASES, ids=[c[0] for c in EDGE_CASES])
+@pytest.mark.parametrize("cell_mult", [1, 2])
+def test_edge_shapes_match_oracle(name, gen, W, S, eps, mp, cell_mult):
+    pts = gen()
+    slides = (len(pts) - W) // S
+    got = run_stream(pts, W, S, eps, mp, slides, cell_mult=cell_mult)
+    exp = O.stream(pts, W, S, eps, mp, O.MODE_FP64, first_slide=1, n_out=slides)
+    assert_same(got[:3], exp, f"{name}/K{cell_mult}")
