@@ -699,6 +699,13 @@ void pool_drop_shape(rtdbs_pool* p) {
     p->plan.clear();
 }
 
+// Phases launched once per stream group: those whose bodies are instantiated
+// per group, and the forest-reuse passes between them (so the increment
+// through the label phase form one run of grouped phases).
+bool pool_grouped(int phase) {
+    return rtdbs::batch_phase_split(phase) || phase == rtdbs::kBatchDamage || phase == rtdbs::kBatchReuse;
+}
+
 // Builds (and uploads) the launch tables of one round over `ids`.
 int pool_build_shape(rtdbs_pool* p, const std::vector<int>& ids) {
     using rtdbs::BatchItem;
@@ -732,7 +739,7 @@ int pool_build_shape(rtdbs_pool* p, const std::vector<int>& ids) {
     // (precision, dim) group present.
     auto add_launches = [&](int ph, const std::vector<BatchItem>& items) {
         std::vector<std::pair<int, int>> groups;
-        if (rtdbs::batch_phase_split(ph)) {
+        if (pool_grouped(ph)) {
             for (const auto& it : items) {
                 const auto& v = p->eng[it.view]->v;
                 const std::pair<int, int> g(v.precision, rtdbs::dk_of(v));
@@ -745,7 +752,7 @@ int pool_build_shape(rtdbs_pool* p, const std::vector<int>& ids) {
             std::vector<BatchItem> sel;
             for (const auto& it : items) {
                 const auto& v = p->eng[it.view]->v;
-                if (!rtdbs::batch_phase_split(ph) || (v.precision == g.first && rtdbs::dk_of(v) == g.second))
+                if (!pool_grouped(ph) || (v.precision == g.first && rtdbs::dk_of(v) == g.second))
                     sel.push_back(it);
             }
             std::vector<int> prefix(sel.size() + 1, 0);
@@ -803,27 +810,43 @@ cudaError_t pool_launch(rtdbs_pool* p, const rtdbs_pool::Launch& l, cudaStream_t
     return rtdbs::launch_batch(l.phase, l.prec, l.dim, L, l.blocks, l.max_c, s);
 }
 
-// One round.  The group launches of a split phase (consecutive plan entries
-// of one phase) are independent -- disjoint streams of the pool -- so they
-// run side by side: the first on the pool's stream, the others on side
-// streams forked from it and joined back before the next phase.
+// One round.  The stream groups' launches of consecutive grouped phases
+// (a segment: the decrement, and the increment through the label phase) are
+// independent -- disjoint streams of the pool -- so each group runs its part
+// of the segment in phase order on its own stream: the first group on the
+// pool's stream, the others on side streams forked from it at the start of
+// the segment and joined back at its end.  Ungrouped phases (ingest, sort,
+// merge, build) take every stream in one launch.
 int pool_enqueue_round(rtdbs_pool* p) {
     const size_t n = p->plan.size();
     for (size_t i = 0; i < n;) {
-        size_t j = i + 1;
-        while (j < n && j - i <= (size_t)rtdbs_pool::kSide && p->plan[j].phase == p->plan[i].phase &&
-               rtdbs::batch_phase_split(p->plan[i].phase))
-            ++j;
-        if (j - i > 1) {
-            CUDA_TRY(cudaEventRecord(p->ev_fork, p->stream));
-            for (size_t g = 1; g < j - i; ++g) {
-                CUDA_TRY(cudaStreamWaitEvent(p->side[g - 1], p->ev_fork, 0));
-                CUDA_TRY(pool_launch(p, p->plan[i + g], p->side[g - 1]));
-                CUDA_TRY(cudaEventRecord(p->ev_join[g - 1], p->side[g - 1]));
-            }
+        if (!pool_grouped(p->plan[i].phase)) {
+            CUDA_TRY(pool_launch(p, p->plan[i], p->stream));
+            ++i;
+            continue;
         }
-        CUDA_TRY(pool_launch(p, p->plan[i], p->stream));
-        for (size_t g = 1; g < j - i; ++g) CUDA_TRY(cudaStreamWaitEvent(p->stream, p->ev_join[g - 1], 0));
+        size_t j = i;
+        std::vector<std::pair<int, int>> groups;
+        while (j < n && pool_grouped(p->plan[j].phase)) {
+            const std::pair<int, int> g(p->plan[j].prec, p->plan[j].dim);
+            if (std::find(groups.begin(), groups.end(), g) == groups.end()) groups.push_back(g);
+            ++j;
+        }
+        const int ng = (int)groups.size();
+        if (ng > 1 + rtdbs_pool::kSide) return fail(RTDBS_ERR_INVALID, "too many stream groups");
+        if (ng > 1) {
+            CUDA_TRY(cudaEventRecord(p->ev_fork, p->stream));
+            for (int g = 1; g < ng; ++g) CUDA_TRY(cudaStreamWaitEvent(p->side[g - 1], p->ev_fork, 0));
+        }
+        for (size_t k = i; k < j; ++k) {
+            const int g = (int)(std::find(groups.begin(), groups.end(),
+                                          std::make_pair(p->plan[k].prec, p->plan[k].dim)) - groups.begin());
+            CUDA_TRY(pool_launch(p, p->plan[k], g == 0 ? p->stream : p->side[g - 1]));
+        }
+        for (int g = 1; g < ng; ++g) {
+            CUDA_TRY(cudaEventRecord(p->ev_join[g - 1], p->side[g - 1]));
+            CUDA_TRY(cudaStreamWaitEvent(p->stream, p->ev_join[g - 1], 0));
+        }
         i = j;
     }
     return RTDBS_OK;
