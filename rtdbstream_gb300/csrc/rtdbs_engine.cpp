@@ -89,6 +89,9 @@ struct rtdbs_engine {
     bool geometry_ready = false;
     bool loaded = false;
     cudaGraphExec_t slide_graph = nullptr;
+    // side stream for the decrement pass beside the sort (made on the first slide)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double cell_side = 0.0;
 };
 
@@ -262,14 +265,25 @@ int enqueue_slide(rtdbs_engine* e) {
     const int nchunks = (S + C - 1) / C;
     for (int j = 0; j < nchunks; ++j) {
         const int c = std::min(C, S - j * C);
-        CUDA_TRY(rtdbs::launch_chunk_step(e->v, e->p.precision, j, c, 0, j * C, e->stream));
+        CUDA_TRY(rtdbs::launch_chunk_step(e->v, e->p.precision, j, c, 0, j * C, e->stream, e->side, e->ev_fork,
+                                          e->ev_join));
     }
     CUDA_TRY(rtdbs::launch_cluster(e->v, e->p.precision, 1, e->stream));
     return RTDBS_OK;
 }
 
 // Enqueues one slide whose new points are already in the staging buffer.
+int ensure_side(rtdbs_engine* e) {
+    if (e->side) return RTDBS_OK;
+    CUDA_TRY(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
+    CUDA_TRY(cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking));
+    return RTDBS_OK;
+}
+
 int run_slide(rtdbs_engine* e) {
+    int rc0 = ensure_side(e);  // before any capture
+    if (rc0 != RTDBS_OK) return rc0;
     if (e->p.flags & RTDBS_FLAG_NO_GRAPH) return enqueue_slide(e);
     if (!e->slide_graph) {
         cudaGraph_t g = nullptr;
@@ -413,6 +427,9 @@ int rtdbs_destroy(rtdbs_engine* e) {
     if (e->slide_graph) cudaGraphExecDestroy(e->slide_graph);
     if (e->dev_block) cudaFree(e->dev_block);
     if (e->h_ctl) cudaFreeHost(e->h_ctl);
+    if (e->side) cudaStreamDestroy(e->side);
+    if (e->ev_fork) cudaEventDestroy(e->ev_fork);
+    if (e->ev_join) cudaEventDestroy(e->ev_join);
     if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
     delete e;
     return RTDBS_OK;
@@ -811,23 +828,51 @@ cudaError_t pool_launch(rtdbs_pool* p, const rtdbs_pool::Launch& l, cudaStream_t
 }
 
 // One round.  The stream groups' launches of consecutive grouped phases
-// (a segment: the decrement, and the increment through the label phase) are
-// independent -- disjoint streams of the pool -- so each group runs its part
-// of the segment in phase order on its own stream: the first group on the
-// pool's stream, the others on side streams forked from it at the start of
-// the segment and joined back at its end.  Ungrouped phases (ingest, sort,
-// merge, build) take every stream in one launch.
+// (the increment through the label phase) are independent -- disjoint
+// streams of the pool -- so each group runs its part of that run in phase
+// order on its own stream: the first group on the pool's stream, the others
+// on side streams forked from it at the start of the run and joined back at
+// its end.  The decrement needs only the ingest, so its group launches run
+// on side streams beside the sort and are joined before the merge.
+// Ungrouped phases (ingest, sort, merge, build) take every stream in one
+// launch.
 int pool_enqueue_round(rtdbs_pool* p) {
     const size_t n = p->plan.size();
+    std::vector<char> done(n, 0);
+    int pending_join = 0;  // side streams running a decrement
     for (size_t i = 0; i < n;) {
-        if (!pool_grouped(p->plan[i].phase)) {
+        if (done[i]) {
+            ++i;
+            continue;
+        }
+        const int ph = p->plan[i].phase;
+        if (!pool_grouped(ph)) {
+            if (ph == rtdbs::kBatchMerge)
+                for (int g = 0; g < pending_join; ++g) CUDA_TRY(cudaStreamWaitEvent(p->stream, p->ev_join[g], 0));
+            if (ph == rtdbs::kBatchMerge) pending_join = 0;
             CUDA_TRY(pool_launch(p, p->plan[i], p->stream));
+            if (ph == rtdbs::kBatchIngest) {
+                // this chunk step's decrement launches, up to the merge
+                std::vector<size_t> dec;
+                for (size_t k = i + 1; k < n && p->plan[k].phase != rtdbs::kBatchMerge; ++k)
+                    if (p->plan[k].phase == rtdbs::kBatchDecrement) dec.push_back(k);
+                if (!dec.empty() && (int)dec.size() <= rtdbs_pool::kSide) {
+                    CUDA_TRY(cudaEventRecord(p->ev_fork, p->stream));
+                    for (size_t g = 0; g < dec.size(); ++g) {
+                        CUDA_TRY(cudaStreamWaitEvent(p->side[g], p->ev_fork, 0));
+                        CUDA_TRY(pool_launch(p, p->plan[dec[g]], p->side[g]));
+                        CUDA_TRY(cudaEventRecord(p->ev_join[g], p->side[g]));
+                        done[dec[g]] = 1;
+                    }
+                    pending_join = (int)dec.size();
+                }
+            }
             ++i;
             continue;
         }
         size_t j = i;
         std::vector<std::pair<int, int>> groups;
-        while (j < n && pool_grouped(p->plan[j].phase)) {
+        while (j < n && pool_grouped(p->plan[j].phase) && !done[j]) {
             const std::pair<int, int> g(p->plan[j].prec, p->plan[j].dim);
             if (std::find(groups.begin(), groups.end(), g) == groups.end()) groups.push_back(g);
             ++j;
@@ -849,6 +894,7 @@ int pool_enqueue_round(rtdbs_pool* p) {
         }
         i = j;
     }
+    for (int g = 0; g < pending_join; ++g) CUDA_TRY(cudaStreamWaitEvent(p->stream, p->ev_join[g], 0));
     return RTDBS_OK;
 }
 

@@ -152,8 +152,11 @@ constexpr int kChunkPhases = 6;  // ingest .. increment, once per chunk
 // advance = 1 when the label phase ends a slide.
 cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, int init,
                          int staging_offset, int advance, cudaStream_t s);
+// With a side stream and two events, the decrement pass (which needs only
+// the ingest) runs on `side` beside the sort, joined before the merge.
 cudaError_t launch_chunk_step(const View& v, int precision, int j, int c, int init,
-                              int staging_offset, cudaStream_t s);
+                              int staging_offset, cudaStream_t s, cudaStream_t side = nullptr,
+                              cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 cudaError_t launch_cluster(const View& v, int precision, int advance, cudaStream_t s);
 cudaError_t launch_counts_by_slot(const View& v, int* nn_by_slot, cudaStream_t s);
 cudaError_t configure_kernels();

@@ -622,9 +622,11 @@ __device__ __forceinline__ void decr_body(const View& v, int j, int c, int bx, S
     const int old = (int)((b - 1) & 1);
     const unsigned gen = gen_of_build(b - 1);
     const int el = chunk_base_slot(v, j, 0);
-    const unsigned long long word = has ? v.xword[qi] : 0ull;
-    const unsigned long long key = word >> kOffBits;
-    const float4 xp = has ? v.xpt[word & ((1u << kOffBits) - 1)] : make_float4(0.f, 0.f, 0.f, 0.f);
+    // Expired points in chunk order, keyed from their saved coordinates (the
+    // same key they were sorted by when they arrived): the pass does not wait
+    // for the chunk's sort, and runs beside it.
+    const float4 xp = has ? v.xpt[qi] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const unsigned long long key = has ? cell_key(v, xp.x, xp.y, xp.z) : 0ull;
     int rs, re;
     row_ranges<DIM, false, K, G>(v, v.table[old], gen, key, gl, rs, re);
     int total = candidate_stream<Stencil<DIM, false, K>::kRows, G>(rs, re, 0, gl, rstart, rpre);
@@ -1658,11 +1660,22 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
 }
 
 cudaError_t launch_chunk_step(const View& v, int precision, int j, int c, int init, int stg_off,
-                              cudaStream_t s) {
+                              cudaStream_t s, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
     if (c <= 0 || c > kChunkMax) return cudaErrorInvalidValue;
+    const bool beside = side && fork && join && !init;  // the decrement beside the sort
     for (int ph = 0; ph < kChunkPhases; ++ph) {
-        const cudaError_t e = launch_phase(ph, v, precision, j, c, init, stg_off, 0, s);
+        cudaError_t e = cudaSuccess;
+        if (beside && ph == kPhaseDecrement) continue;  // launched right after the ingest
+        if (beside && ph == kPhaseMerge && (e = cudaStreamWaitEvent(s, join, 0)) != cudaSuccess) return e;
+        e = launch_phase(ph, v, precision, j, c, init, stg_off, 0, s);
         if (e != cudaSuccess) return e;
+        if (beside && ph == kPhaseIngest) {
+            if ((e = cudaEventRecord(fork, s)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(side, fork, 0)) != cudaSuccess) return e;
+            if ((e = launch_phase(kPhaseDecrement, v, precision, j, c, init, stg_off, 0, side)) != cudaSuccess)
+                return e;
+            if ((e = cudaEventRecord(join, side)) != cudaSuccess) return e;
+        }
     }
     return cudaSuccess;
 }
