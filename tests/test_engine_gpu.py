@@ -245,13 +245,14 @@ def reuse_stream(seed=21):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_forest_reuse_matches_oracle(precision):
+@pytest.mark.parametrize("cell_mult", [1, 2])
+def test_forest_reuse_matches_oracle(precision, cell_mult):
     pts, W, S = reuse_stream()
     eps, mp = 0.25, 5
-    got = run_stream(pts, W, S, eps, mp, 4, precision=precision)
+    got = run_stream(pts, W, S, eps, mp, 4, precision=precision, cell_mult=cell_mult)
     mode = O.MODE_FP64 if precision == "fp64" else O.MODE_FP32
     exp = O.stream(pts, W, S, eps, mp, mode, first_slide=1, n_out=4)
-    assert_same(got[:3], exp, f"reuse/{precision}")
+    assert_same(got[:3], exp, f"reuse/{precision}/K{cell_mult}")
     # the blob components were kept from the previous slide
     assert got[3]["reused_cores"] > 1_000
     # the bridge expired in the last slide: the two blobs it joined split
