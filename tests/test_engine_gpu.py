@@ -226,6 +226,34 @@ def test_walkers_full_window_exact():
     assert_same(got[:3], exp, "walkers 1M")
 
 
+def test_precision_config_full_size():
+    """The precision configuration at full size (W = 500k, S = 5k, large
+    common offset, 5% of points at Eps(1 +- 1e-6) from an anchor): labels,
+    ids and counts equal the FP64 oracle, FP64 re-checks happen, and the
+    FP64 relation really differs from the reference's FP32 one here."""
+    spec = wl.CFG2
+    pts = wl.cfg2_stream(n_total=spec.window + 3 * spec.stride)
+    got = run_stream(pts, spec.window, spec.stride, spec.eps, spec.min_pts, 3)
+    exp = O.stream(pts, spec.window, spec.stride, spec.eps, spec.min_pts, O.MODE_FP64, first_slide=1, n_out=3)
+    assert_same(got[:3], exp, "offset 500k")
+    assert got[3]["band_rechecks"] > 0
+    e32 = O.stream(pts, spec.window, spec.stride, spec.eps, spec.min_pts, O.MODE_FP32, first_slide=1, n_out=3)
+    assert not np.array_equal(exp[0], e32[0])
+
+
+def test_mixture_config_all_slides():
+    """The 2-D mixture configuration as specified: W = 10k, S = 1k, all 100
+    slides, every window equal to the FP64 oracle and, in FP32 mode, to the
+    reference semantics."""
+    spec = wl.CFG0
+    pts = wl.cfg0_stream()
+    for precision, mode in (("fp64", O.MODE_FP64), ("fp32", O.MODE_FP32)):
+        got = run_stream(pts, spec.window, spec.stride, spec.eps, spec.min_pts, spec.slides, precision=precision)
+        exp = O.stream(pts, spec.window, spec.stride, spec.eps, spec.min_pts, mode, first_slide=1,
+                       n_out=spec.slides)
+        assert_same(got[:3], exp, f"mixture W10k/{precision}")
+
+
 def reuse_stream(seed=21):
     """A window whose oldest points are far-away noise and a bridge between
     two blobs, its newest points three stationary 2-D blobs: the first slides
