@@ -105,3 +105,32 @@ def test_stream_bytes_without_device():
     # MinPts above the longest list kept: no list buffers
     no_lists = E.stream_bytes(E.make_params(3, 1_000_000, 10_000, 3.3e-3, 40))
     assert 120 * 1_000_000 < no_lists <= b - 40 * 1_000_000
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors have the C structs' sizes and field offsets (a C
+    compiler reads include/rtdbs.h)."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    structs = {"rtdbs_params": E.Params, "rtdbs_stats": E.Stats, "rtdbs_phase_times": E.PhaseTimes,
+               "rtdbs_pool_params": E.PoolParams, "rtdbs_pool_stats": E.PoolStats}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "rtdbs.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'    printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'    printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
