@@ -225,6 +225,7 @@ size_t plan_layout(rtdbs_engine* e, std::vector<Part>& parts) {
         {(void**)&v.nword, sizeof(unsigned long long) * C},
         {(void**)&v.xword, sizeof(unsigned long long) * C},
         {(void**)&v.xpt, sizeof(float4) * C},
+        {(void**)&v.sorder, sizeof(int) * W},
         {(void**)&v.staging, sizeof(float) * (size_t)e->staging_points * dim},
         {(void**)&v.ctl, sizeof(Ctl)},
     };

@@ -125,6 +125,9 @@ struct View {
     unsigned long long* nword;   // sorted
     unsigned long long* xword;
     float4* xpt;                 // expired points of the chunk by offset
+    int* sorder;                 // per slot el + r: offset (slot - el) of the chunk's r-th
+                                 // point in (key, slot) order, kept from the slide that
+                                 // brought the chunk in; null: not kept
     const float* staging;        // new points [S][dim]
     Ctl* ctl;
 };

@@ -82,6 +82,14 @@ __device__ __forceinline__ int chunk_base_slot(const View& v, int j, int init) {
     return base + j * v.chunk;
 }
 
+// The expiring chunk's (key, slot) order is known from the slide that
+// brought it in (sorder), so its words need no sort: true once every slot of
+// the window arrived by a slide (the first window's load chunks tile the
+// slots differently).  Keys do not change while a point is in the window.
+__device__ __forceinline__ bool expired_presorted(const View& v, int init) {
+    return !init && v.sorder != nullptr && v.ctl->slide >= (long long)v.units;
+}
+
 // ----------------------------------------------------------------- predicate
 
 template <int DIM>
@@ -501,7 +509,7 @@ __device__ __forceinline__ void sort_body(const View& v, int c, int init, int bx
     unsigned* whist = sm.whist;
     unsigned* wsum = sm.wsum;
     const int which = by;
-    if (which == 1 && init) return;
+    if (which == 1 && (init || expired_presorted(v, init))) return;
     const int r0 = bx * kSortRun;
     const int len = min(kSortRun, c - r0);
     if (len <= 0) return;
@@ -554,11 +562,24 @@ __global__ void __launch_bounds__(kSortRun) k_sort(View v, int c, int init) {
 // rank is its index in its run plus the words below it in every other run
 // (words are distinct, so ranks are too).  Block (r, y) ranks run r of the
 // new (y = 0) or expired (y = 1) words; all c words are staged in shared
-// memory first, so the binary searches stay on chip.
-__device__ __forceinline__ void runmerge_body(const View& v, int c, int init, int bx, int by,
+// memory first, so the binary searches stay on chip.  Presorted expired
+// words are gathered in their kept order instead.
+__device__ __forceinline__ void runmerge_body(const View& v, int j, int c, int init, int bx, int by,
                                               unsigned long long* words) {
     const int which = by;
     if (which == 1 && init) return;
+    if (which == 1 && expired_presorted(v, init)) {
+        const int i = bx * kSortRun + threadIdx.x;
+        if (i >= c) return;
+        const int k = v.sorder[chunk_base_slot(v, j, 0) + i];
+        if (k < 0 || k >= c) {
+            atomicOr(&v.ctl->err, kErrChunk);
+            v.xword[i] = ~0ull;
+            return;
+        }
+        v.xword[i] = v.xsort[k];
+        return;
+    }
     const unsigned long long* runs = which ? v.xsort : v.nsort;
     unsigned long long* out = which ? v.xword : v.nword;
     for (int i = threadIdx.x; i < c; i += blockDim.x) words[i] = runs[i];
@@ -585,9 +606,9 @@ __device__ __forceinline__ void runmerge_body(const View& v, int c, int init, in
     out[rank] = w;
 }
 
-__global__ void __launch_bounds__(kSortRun) k_runmerge(View v, int c, int init) {
+__global__ void __launch_bounds__(kSortRun) k_runmerge(View v, int j, int c, int init) {
     extern __shared__ unsigned long long words[];
-    runmerge_body(v, c, init, blockIdx.x, blockIdx.y, words);
+    runmerge_body(v, j, c, init, blockIdx.x, blockIdx.y, words);
 }
 
 // -1 on the count of every surviving neighbour of each expired point (old grid).
@@ -615,17 +636,26 @@ __device__ __forceinline__ void decr_body(const View& v, int j, int c, int bx, S
     const int gw = (bx * blockDim.x + threadIdx.x) >> 5;
     if (gw * kPerWarp >= c) return;
     const int qi = gw * kPerWarp + grp;
-    const bool has = qi < c;
+    bool has = qi < c;
     int* rstart = sm.grstart[wib][grp];
     int* rpre = sm.grpre[wib][grp];
     const long long b = v.ctl->b;
     const int old = (int)((b - 1) & 1);
     const unsigned gen = gen_of_build(b - 1);
     const int el = chunk_base_slot(v, j, 0);
-    // Expired points in chunk order, keyed from their saved coordinates (the
-    // same key they were sorted by when they arrived): the pass does not wait
-    // for the chunk's sort, and runs beside it.
-    const float4 xp = has ? v.xpt[qi] : make_float4(0.f, 0.f, 0.f, 0.f);
+    // Expired points keyed from their saved coordinates (the same key they
+    // were sorted by when they arrived): the pass does not wait for the
+    // chunk's sort, and runs beside it.  Taken in their kept (key, slot)
+    // order where there is one, so neighbouring warps read the same cells.
+    int k = qi;
+    if (has && expired_presorted(v, 0)) {
+        k = v.sorder[el + qi];
+        if (k < 0 || k >= c) {
+            atomicOr(&v.ctl->err, kErrChunk);
+            has = false;
+        }
+    }
+    const float4 xp = has ? v.xpt[k] : make_float4(0.f, 0.f, 0.f, 0.f);
     const unsigned long long key = has ? cell_key(v, xp.x, xp.y, xp.z) : 0ull;
     int rs, re;
     row_ranges<DIM, false, K, G>(v, v.table[old], gen, key, gl, rs, re);
@@ -866,6 +896,9 @@ __device__ __forceinline__ void merge_body(const View& v, int j, int c, int init
         dcnt[o] = 0;
         v.sroot[o] = slot;
         if (reset_parent) v.parent[slot] = slot;
+        // the chunk's order, for the slide that expires it (every reader of
+        // the expired order of these slots ran before this pass)
+        if (!init && v.sorder) v.sorder[el + q] = slot - el;
     }
 }
 
@@ -1515,7 +1548,7 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
     } else if constexpr (PHASE == kBatchRunmerge) {
         extern __shared__ unsigned long long words[];
         const int nruns = (it.c + kSortRun - 1) / kSortRun;
-        runmerge_body(sv, it.c, 0, bx % nruns, bx / nruns, words);
+        runmerge_body(sv, it.j, it.c, 0, bx % nruns, bx / nruns, words);
     } else if constexpr (PHASE == kBatchDecrement) {
         __shared__ StreamSmem sm;
         decr_body<MODE, DK>(sv, it.j, it.c, bx, sm);
@@ -1610,7 +1643,7 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
             k_sort<<<dim3((c + kSortRun - 1) / kSortRun, init ? 1 : 2), kSortRun, 0, s>>>(v, c, init);
             ensure_runmerge_smem();
             k_runmerge<<<dim3((c + kSortRun - 1) / kSortRun, init ? 1 : 2), kSortRun,
-                         sizeof(unsigned long long) * c, s>>>(v, c, init);
+                         sizeof(unsigned long long) * c, s>>>(v, j, c, init);
             break;
         case kPhaseDecrement:
             if (!init) RTDBS_DISPATCH(precision, dk_of(v), k_decr, warp_blocks, 256, s, v, j, c);

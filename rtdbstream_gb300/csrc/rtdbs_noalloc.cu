@@ -215,7 +215,7 @@ extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int
     v.max_items = kMaxItems;
     v.list_cap = -1;  // no neighbour lists: the label pass scans the grid
     v.list_stride = 0;
-    v.nlist = v.ntrack = v.rslot = v.damaged = nullptr;
+    v.nlist = v.ntrack = v.rslot = v.damaged = v.sorder = nullptr;
 
     v.ring = reinterpret_cast<float4*>(base + kOffRing);
     v.kslot = reinterpret_cast<unsigned long long*>(base + kOffKslot);

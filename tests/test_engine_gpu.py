@@ -327,3 +327,50 @@ def test_edge_shapes_match_oracle(name, gen, W, S, eps, mp, cell_mult):
     got = run_stream(pts, W, S, eps, mp, slides, cell_mult=cell_mult)
     exp = O.stream(pts, W, S, eps, mp, O.MODE_FP64, first_slide=1, n_out=slides)
     assert_same(got[:3], exp, f"{name}/K{cell_mult}")
+
+
+# Streams slid past W/S slides: every expiring chunk then arrived by a slide,
+# so its (key, slot) order is the one kept from that slide and its words are
+# not sorted again.  Covers one and two sort chunks per slide, S = 1 and
+# S = W, both cell multipliers and both predicates.
+STEADY_CASES = [
+    ("mix2d_W2k_S200", lambda: wl.gaussian_mixture(2_000 + 25 * 200, dim=2, k=6, box=20.0, seed=51),
+     2_000, 200, 0.5, 5, 25),
+    ("walk3d_W6k_S1k", lambda: wl.random_walkers(6_000 + 14 * 1_000, n_walkers=40, seed=52), 6_000, 1_000,
+     3.3e-3, 10, 14),
+    ("two_chunks_W40k_S20k", lambda: wl.gaussian_mixture(40_000 + 5 * 20_000, dim=2, k=30, box=100.0, seed=53),
+     40_000, 20_000, 0.4, 6, 5),
+    ("S1_W16_2d", lambda: wl.gaussian_mixture(16 + 40, dim=2, k=2, box=2.0, seed=54), 16, 1, 0.5, 3, 40),
+    ("S_eq_W_2d", lambda: wl.gaussian_mixture(1_500 * 5, dim=2, k=4, box=12.0, seed=55), 1_500, 1_500, 0.5, 4, 4),
+]
+
+
+@pytest.mark.parametrize("name,gen,W,S,eps,mp,slides", STEADY_CASES, ids=[c[0] for c in STEADY_CASES])
+@pytest.mark.parametrize("precision,cell_mult", [("fp64", 1), ("fp32", 1), ("fp64", 2)])
+def test_steady_state_streams_match_oracle(name, gen, W, S, eps, mp, slides, precision, cell_mult):
+    assert slides > W // S
+    pts = gen()
+    got = run_stream(pts, W, S, eps, mp, slides, precision=precision, cell_mult=cell_mult)
+    mode = O.MODE_FP64 if precision == "fp64" else O.MODE_FP32
+    exp = O.stream(pts, W, S, eps, mp, mode, first_slide=1, n_out=slides)
+    assert_same(got[:3], exp, f"{name}/{precision}/K{cell_mult}")
+    assert got[3]["error_bits"] == 0
+
+
+def test_reload_after_steady_state():
+    """A new first window loaded into an engine that already slid past W/S
+    slides starts over: its first W/S slides sort the expired words again."""
+    W, S, eps, mp = 1_200, 300, 0.5, 5
+    a = wl.gaussian_mixture(W + 9 * S, dim=2, k=5, box=15.0, seed=56)
+    b = wl.gaussian_mixture(W + 7 * S, dim=2, k=5, box=15.0, seed=57)
+    with Engine(2, W, S, eps, mp) as eng:
+        eng.load_window(a[:W])
+        for k in range(9):
+            eng.slide(a[W + k * S: W + (k + 1) * S])
+        eng.load_window(b[:W])
+        got = []
+        for k in range(7):
+            lab, cid = eng.slide(b[W + k * S: W + (k + 1) * S])
+            got.append((eng.counts(), lab, cid))
+    exp = O.stream(b, W, S, eps, mp, O.MODE_FP64, first_slide=1, n_out=7)
+    assert_same(tuple(np.array(x) for x in zip(*got)), exp, "reloaded")

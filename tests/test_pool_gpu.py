@@ -182,3 +182,38 @@ def test_pool_mixes_cell_multipliers():
             win = O.window_of(d, W, S, ROUNDS)
             _, olab, ocid, _ = O.window_grid(win, eps, mp, O.MODE_FP64)
             assert np.array_equal(lab, olab) and np.array_equal(cid, ocid)
+
+
+def test_pool_steady_state_rounds():
+    """Pool streams slid past W/S rounds (expired chunks in their kept order,
+    not sorted again), one of them sitting out every third round, against the
+    oracle after each round."""
+    import torch
+
+    specs = [(2, 1_000, 100, 0.5, 5, 1), (3, 2_400, 800, 0.8, 6, 1), (2, 1_200, 150, 0.5, 4, 2)]
+    rounds = 16
+    data = [wl.gaussian_mixture(W + rounds * S, dim=dim, k=5, box=15.0, seed=310 + i)
+            for i, (dim, W, S, eps, mp, km) in enumerate(specs)]
+    done = [0] * len(specs)
+    with Pool() as pool:
+        ids = []
+        for (dim, W, S, eps, mp, km), d in zip(specs, data):
+            sid = pool.add_stream(make_params(dim, W, S, eps, mp, cell_mult=km))
+            pool.load_window(sid, d[:W])
+            ids.append(sid)
+        for r in range(rounds):
+            members = [i for i in range(len(specs)) if not (i == 1 and r % 3 == 2)]
+            buf = torch.from_numpy(np.concatenate([data[i][specs[i][1] + done[i] * specs[i][2]:
+                                                           specs[i][1] + (done[i] + 1) * specs[i][2]].reshape(-1)
+                                                   for i in members])).cuda()
+            pool.slide([ids[i] for i in members], buf)
+            pool.sync()
+            for i in members:
+                done[i] += 1
+                dim, W, S, eps, mp, km = specs[i]
+                win = O.window_of(data[i], W, S, done[i])
+                enn, elab, ecid, _ = O.window_grid(win, eps, mp, O.MODE_FP64)
+                lab, cid = pool.outputs(ids[i])
+                assert np.array_equal(lab, elab) and np.array_equal(cid, ecid), f"stream {i} round {r}"
+                assert np.array_equal(pool.counts(ids[i]), enn), f"stream {i} round {r}: counts"
+    assert min(done) > max(W // S for dim, W, S, *_ in specs)
