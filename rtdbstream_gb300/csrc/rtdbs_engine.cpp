@@ -581,7 +581,7 @@ int rtdbs_get_stats(rtdbs_engine* e, rtdbs_stats* s) {
     s->chunks_per_slide = nchunks;
     // sort phase = 2 kernels; with neighbour lists the union phase adds the
     // two forest-reuse passes
-    s->launches_per_slide = nchunks * (rtdbs::kChunkPhases + 1) + 3 + (e->v.list_cap >= 0 ? 2 : 0);
+    s->launches_per_slide = nchunks * (rtdbs::kChunkPhases + 1) + 4 + (e->v.list_cap >= 0 ? 1 : 0);
     return RTDBS_OK;
 }
 

@@ -111,8 +111,8 @@ struct View {
     ulonglong2* table[2];
     int2* items;
     int* parent;
-    int* sroot;                  // per sorted position: root hint during the union,
-                                 // then the root (-1: not core)
+    int* sroot;                  // per sorted position: root hint during the union
+                                 // (-1: not core), then the root (-1: not core)
     int* label;
     int* cid;
     int* nlist;                  // [W][list_stride] neighbours of non-core points

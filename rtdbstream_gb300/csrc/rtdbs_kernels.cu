@@ -1111,16 +1111,22 @@ __device__ __forceinline__ void damage_body(const View& v, int bx, int nbx) {
     }
 }
 
-// Cores of intact components join their old root (parent and hint).
+// Marks every non-core position's hint -1 (the union then tells cores from
+// their hint alone), and, with neighbour lists, lets the cores of intact
+// components join their old root (parent and hint).
 __device__ __forceinline__ void reuse_body(const View& v, int bx, int nbx) {
-    if (!v.ctl->prev_ok || v.ctl->reuse_skip > 0) return;
+    const bool reuse_on = v.list_cap >= 0 && v.ctl->prev_ok && v.ctl->reuse_skip <= 0;
     const int cur = (int)(v.ctl->b & 1);
     const int n = v.ctl->nocc[cur];
     const int* scnt = v.scnt[cur];
     const int* sw = reinterpret_cast<const int*>(v.spt[cur]) + 3;
     unsigned reused = 0;
     for (int i = bx * blockDim.x + threadIdx.x; i < n; i += nbx * blockDim.x) {
-        if (scnt[i] < v.min_pts) continue;
+        if (scnt[i] < v.min_pts) {
+            v.sroot[i] = -1;
+            continue;
+        }
+        if (!reuse_on) continue;
         const int s = sw[4 * (size_t)i];
         if (v.label[s] != 0 || slot_is_new(v, s)) continue;
         const int r = v.cid[s];
@@ -1164,12 +1170,12 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
     const unsigned gen = gen_of_build(b);
     const int nitems = min(v.ctl->nitems, v.max_items);
     const float4* spt = v.spt[cur];
-    const int* scnt = v.scnt[cur];
     const unsigned long long* skey = v.skey[cur];
     const ulonglong2* T = v.table[cur];
     int* parent = v.parent;
     // Root hints by sorted position (an ancestor of the point; the merge sets
-    // each to the point's own slot): coalesced with the candidate loads, and
+    // each to the point's own slot, k_reuse marks non-core points -1, so the
+    // hint alone tells a core): coalesced with the candidate loads, and
     // refreshed as roots are found, so find walks stay short.
     volatile int* hint = v.sroot;
     Tally tally;
@@ -1191,14 +1197,15 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
         const bool hv = lane < len;
         float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
         bool hcore = false;
+        int hh = -1;
         if (hv) {
             h = spt[start + lane];
-            hcore = scnt[start + lane] >= v.min_pts;
+            hh = hint[start + lane];
+            hcore = hh >= 0;
         }
         const unsigned hmask = __ballot_sync(kFull, hcore);
         if (!hmask) continue;
         __syncwarp();
-        const int hh = hcore ? hint[start + lane] : 0;
         if (hcore) rh[lane] = hh;
         home_pt[wib][lane] = h;
         // All home cores under one hint r0 (common once the previous forest is
@@ -1218,10 +1225,9 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
             bool qc = false;
             if (idx < total) {
                 pos = stream_pos(idx, r, rstart[wib], rpre[wib]);
-                const int qn = scnt[pos];
                 q = spt[pos];
                 qh = hint[pos];
-                qc = qn >= v.min_pts;
+                qc = qh >= 0;
             }
             if (!__any_sync(kFull, qc && !(uni && qh == r0))) continue;
             // Pairs whose hints already agree are in one set: no test, no link.
@@ -1564,7 +1570,7 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
     } else if constexpr (PHASE == kBatchDamage) {
         if (sv.list_cap >= 0) damage_body(sv, bx, nbx);
     } else if constexpr (PHASE == kBatchReuse) {
-        if (sv.list_cap >= 0) reuse_body(sv, bx, nbx);
+        reuse_body(sv, bx, nbx);
     } else if constexpr (PHASE == kBatchUnion) {
         __shared__ ClusterSmem sm;
         union_body<MODE, DK>(sv, sm);
@@ -1665,10 +1671,10 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
             }
             [[fallthrough]];
         case kPhaseUnion: {
-            if (v.list_cap >= 0) {
+            {
                 const int sms0 = g_num_sms > 0 ? g_num_sms : 152;
                 const int rb = max(1, min(sms0 * 8, (v.W + 255) / 256));
-                k_damage<<<rb, 256, 0, s>>>(v);
+                if (v.list_cap >= 0) k_damage<<<rb, 256, 0, s>>>(v);
                 k_reuse<<<rb, 256, 0, s>>>(v);
             }
             const int sms = g_num_sms > 0 ? g_num_sms : 152;
@@ -1742,8 +1748,8 @@ int batch_blocks(int phase, const View& v, int c) {
         case kBatchIncrement: return (c * query_lanes(v.cell_mult) + 255) / 256;
         case kBatchMerge: return (v.W + kMergeTile - 1) / kMergeTile;
         case kBatchBuild: return (v.W + kBuildThreads - 1) / kBuildThreads;
-        case kBatchDamage:
-        case kBatchReuse: return v.list_cap >= 0 ? max(1, min(1024, (v.W + 2047) / 2048)) : 0;
+        case kBatchDamage: return v.list_cap >= 0 ? max(1, min(1024, (v.W + 2047) / 2048)) : 0;
+        case kBatchReuse: return max(1, min(1024, (v.W + 2047) / 2048));
         case kBatchUnion: return max(1, min(1024, (v.W + 1023) / 1024));  // persistent, queue-fed
         case kBatchLabel:
             if (v.list_cap >= 0) return max(1, min(1024, (v.W + 1023) / 1024));  // k_border
