@@ -1671,7 +1671,7 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
             }
             [[fallthrough]];
         case kPhaseUnion: {
-            {
+            if (phase == kPhaseUnion) {  // (the label phase without lists falls through)
                 const int sms0 = g_num_sms > 0 ? g_num_sms : 152;
                 const int rb = max(1, min(sms0 * 8, (v.W + 255) / 256));
                 if (v.list_cap >= 0) k_damage<<<rb, 256, 0, s>>>(v);
