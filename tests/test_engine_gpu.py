@@ -342,6 +342,9 @@ STEADY_CASES = [
      40_000, 20_000, 0.4, 6, 5),
     ("S1_W16_2d", lambda: wl.gaussian_mixture(16 + 40, dim=2, k=2, box=2.0, seed=54), 16, 1, 0.5, 3, 40),
     ("S_eq_W_2d", lambda: wl.gaussian_mixture(1_500 * 5, dim=2, k=4, box=12.0, seed=55), 1_500, 1_500, 0.5, 4, 4),
+    # MinPts above the list cap: the label pass scans the grid
+    ("mp40_W2k_S200", lambda: wl.gaussian_mixture(2_000 + 24 * 200, dim=2, k=5, box=15.0, seed=58),
+     2_000, 200, 0.8, 40, 24),
 ]
 
 

@@ -217,3 +217,33 @@ def test_pool_steady_state_rounds():
                 assert np.array_equal(lab, elab) and np.array_equal(cid, ecid), f"stream {i} round {r}"
                 assert np.array_equal(pool.counts(ids[i]), enn), f"stream {i} round {r}: counts"
     assert min(done) > max(W // S for dim, W, S, *_ in specs)
+
+
+def test_pool_mixes_list_and_grid_label_streams():
+    """Streams with MinPts above the neighbour-list cap (label pass scans the
+    grid, no forest reuse) next to list streams in one pool, over enough
+    rounds to pass W/S: each equals the oracle after every round."""
+    import torch
+
+    specs = [(2, 1_500, 150, 0.8, 40, "fp64"), (2, 1_500, 150, 0.5, 5, "fp64"), (3, 2_000, 250, 1.2, 36, "fp32"),
+             (3, 2_000, 250, 0.8, 6, "fp32")]
+    rounds = 12
+    data = [wl.gaussian_mixture(W + rounds * S, dim=dim, k=4, box=12.0, seed=330 + i)
+            for i, (dim, W, S, eps, mp, prec) in enumerate(specs)]
+    with Pool() as pool:
+        ids = []
+        for (dim, W, S, eps, mp, prec), d in zip(specs, data):
+            sid = pool.add_stream(make_params(dim, W, S, eps, mp, precision=prec))
+            pool.load_window(sid, d[:W])
+            ids.append(sid)
+        for r in range(rounds):
+            buf = torch.from_numpy(np.concatenate([d[W + r * S: W + (r + 1) * S].reshape(-1)
+                                                   for (dim, W, S, eps, mp, prec), d in zip(specs, data)])).cuda()
+            pool.slide(ids, buf)
+            pool.sync()
+            for sid, (dim, W, S, eps, mp, prec), d in zip(ids, specs, data):
+                mode = O.MODE_FP64 if prec == "fp64" else O.MODE_FP32
+                enn, elab, ecid, _ = O.window_grid(O.window_of(d, W, S, r + 1), eps, mp, mode)
+                lab, cid = pool.outputs(sid)
+                assert np.array_equal(pool.counts(sid), enn), f"MinPts {mp} round {r}: counts"
+                assert np.array_equal(lab, elab) and np.array_equal(cid, ecid), f"MinPts {mp} round {r}"
