@@ -384,23 +384,42 @@ __device__ __forceinline__ void flush_stats(const View& v, const Tally& t, int e
 // its list rebuilt by one scan.  The label pass then reads lists instead of
 // scanning the grid.
 
+// First index of `x` among the four entries of e (base: index of e.x), or -1.
+__device__ __forceinline__ int find4(const int4& e, int x, int base) {
+    return e.x == x ? base : e.y == x ? base + 1 : e.z == x ? base + 2 : e.w == x ? base + 3 : -1;
+}
+
 // Appends slot p to q's list (q tracked); a full list means q has reached
-// MinPts, so it stops being kept.
+// MinPts, so it stops being kept.  A list row is read 16 bytes at a time
+// from L2 (other SMs may have just written it).  The append claims the first
+// free entry by CAS and looks again if another point took it first; a row
+// still contended after a few looks also stops being kept (the flatten pass
+// rebuilds it).  Padding entries past the cap stay -1 and are never claimed.
 __device__ __forceinline__ void list_append(const View& v, int q, int p) {
     int* L = v.nlist + (size_t)q * v.list_stride;
-    for (int k = 0; k < v.list_cap; ++k)
-        if (L[k] == -1 && atomicCAS(&L[k], -1, p) == -1) return;
+    const int4* L4 = reinterpret_cast<const int4*>(L);
+    const int n4 = v.list_stride >> 2;
+    for (int look = 0; look < 4; ++look) {
+        int k = -1;
+        for (int b = 0; b < n4 && k < 0; ++b) k = find4(__ldcg(L4 + b), -1, 4 * b);
+        if (k < 0 || k >= v.list_cap) break;
+        if (atomicCAS(&L[k], -1, p) == -1) return;
+    }
     v.ntrack[q] = 0;
 }
 
 // Removes slot p from q's list (q tracked; only this thread removes p).
 __device__ __forceinline__ void list_remove(const View& v, int q, int p) {
     int* L = v.nlist + (size_t)q * v.list_stride;
-    for (int k = 0; k < v.list_cap; ++k)
-        if (L[k] == p) {
+    const int4* L4 = reinterpret_cast<const int4*>(L);
+    const int n4 = v.list_stride >> 2;
+    for (int b = 0; b < n4; ++b) {
+        const int k = find4(__ldcg(L4 + b), p, 4 * b);
+        if (k >= 0) {
             L[k] = -1;
             return;
         }
+    }
     atomicOr(&v.ctl->err, kErrList);
 }
 
