@@ -377,3 +377,27 @@ def test_reload_after_steady_state():
             got.append((eng.counts(), lab, cid))
     exp = O.stream(b, W, S, eps, mp, O.MODE_FP64, first_slide=1, n_out=7)
     assert_same(tuple(np.array(x) for x in zip(*got)), exp, "reloaded")
+
+
+def duplicate_points(n, dim, seed):
+    """n points on n // 3 distinct locations, each taken three times, shuffled."""
+    rng = np.random.default_rng(seed)
+    base = rng.uniform(-5.0, 5.0, size=(n // 3 + 1, dim)).astype(np.float32)
+    pts = np.repeat(base, 3, axis=0)[:n]
+    return pts[rng.permutation(n)]
+
+
+# Eps beyond the data's extent (every point in one cell, all pairs tested;
+# Eps^2 above 2^100 turns the FP32 filter off) and below any distance but 0
+# (Eps^2 below 2^-100: the filter is off, only duplicates are neighbours).
+@pytest.mark.parametrize("eps", [50.0, 1e16, 1e-31], ids=["eps_beyond_extent", "eps_1e16", "eps_1e-31"])
+@pytest.mark.parametrize("precision,cell_mult", [("fp64", 1), ("fp32", 1), ("fp64", 2)])
+def test_extreme_eps_match_oracle(eps, precision, cell_mult):
+    W, S, mp, slides = 600, 100, 3, 8
+    pts = duplicate_points(W + slides * S, 3, seed=61)
+    got = run_stream(pts, W, S, eps, mp, slides, precision=precision, cell_mult=cell_mult)
+    mode = O.MODE_FP64 if precision == "fp64" else O.MODE_FP32
+    exp = O.stream(pts, W, S, eps, mp, mode, first_slide=1, n_out=slides)
+    assert_same(got[:3], exp, f"eps {eps}/{precision}/K{cell_mult}")
+    if eps > 1.0:
+        assert np.all(got[1] == 0)  # one cluster of cores
