@@ -430,7 +430,8 @@ def run_batched(args, dev, stream, flush, n_streams=256, rounds=None, plain_roun
     for st, d in zip(streams, data):
         c = tuned[len(ids)]
         sid = pool.add_stream(make_params(st.dim, st.window, st.stride, st.eps, st.min_pts, device=dev,
-                                          cell_mult=c["cell_mult"], work_grab=c["work_grab"]))
+                                          cell_mult=c["cell_mult"], work_grab=c["work_grab"],
+                                          query_lanes=c["query_lanes"]))
         pool.load_window(sid, d[:st.window])
         ids.append(sid)
     for k in range(args.warmup):
@@ -476,7 +477,7 @@ def run_batched(args, dev, stream, flush, n_streams=256, rounds=None, plain_roun
         engines = []
         for st, d, c in zip(streams, data, configs):
             e = Engine(st.dim, st.window, st.stride, st.eps, st.min_pts, device=dev, stream=stream.cuda_stream,
-                       cell_mult=c["cell_mult"], work_grab=c["work_grab"])
+                       cell_mult=c["cell_mult"], work_grab=c["work_grab"], query_lanes=c["query_lanes"])
             e.load_window(d[:st.window])
             engines.append(e)
         ms = []
@@ -495,7 +496,7 @@ def run_batched(args, dev, stream, flush, n_streams=256, rounds=None, plain_roun
         return statistics.mean(ms)
 
     plain_ms = [plain_round_ms(tuned_plain)]
-    default_ms = plain_round_ms([{"cell_mult": 1, "work_grab": 8}] * len(streams))
+    default_ms = plain_round_ms([{"cell_mult": 1, "work_grab": 8, "query_lanes": 16}] * len(streams))
     plain_value = slid / (statistics.mean(plain_ms) / 1000.0)
     return {
         "workload": f"{n_streams} streams, dim 2/3, W log-uniform 1k..200k (sum {sum(st.window for st in streams):,}),"
@@ -505,15 +506,17 @@ def run_batched(args, dev, stream, flush, n_streams=256, rounds=None, plain_roun
         "plain_one_at_a_time": {"value": plain_value, "round_ms": statistics.mean(plain_ms),
                                 "config": "autotuned per stream bucket on single-engine slides"},
         "plain_one_at_a_time_default": {"value": slid / (default_ms / 1000.0), "round_ms": default_ms,
-                                        "config": "1 cell per Eps, 8 items per grab"},
+                                        "config": "1 cell per Eps, 8 items per grab, 16 lanes per count query"},
         "speedup_vs_plain": value / plain_value,
         "launches_per_round": stats["launches_per_round"], "graph_replays": stats["graph_replays"],
         "phase_ms": prof,
         "exact_sample_vs_fp64_oracle": exact,
         "autotune": {"buckets": len(tuner.cache), "tuned_now": tuner.tuned, "tune_s": round(tuner.tune_seconds, 2),
-                     "choices": {k: [v["cell_mult"], v["work_grab"]] for k, v in sorted(tuner.cache.items())
+                     "choices": {k: [v["cell_mult"], v["work_grab"], v.get("query_lanes")]
+                                 for k, v in sorted(tuner.cache.items())
                                  if k.startswith("pool:")},
-                     "plain_choices": {k: [v["cell_mult"], v["work_grab"]] for k, v in sorted(tuner.cache.items())
+                     "plain_choices": {k: [v["cell_mult"], v["work_grab"], v.get("query_lanes")]
+                                       for k, v in sorted(tuner.cache.items())
                                        if not k.startswith("pool:")}},
     }
 

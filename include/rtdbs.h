@@ -95,7 +95,12 @@ typedef struct rtdbs_params {
     int32_t work_grab;    /* work items (cell runs) a clustering warp takes from the shared
                              queue at a time, 1..64 (0 = 8): the work split between warps,
                              picked by rtdbstream_gb300/autotune.py.  No reference counterpart */
-    int32_t reserved[4];
+    int32_t query_lanes;  /* lanes that scan one expired or new point's neighbourhood in the
+                             count passes, 16 or 32 (0 = 16 with one cell per Eps, 32 with
+                             two; two cells per Eps needs 32): the block shape of those
+                             passes (a 256-thread block takes 16 or 8 points), picked by
+                             rtdbstream_gb300/autotune.py.  No reference counterpart */
+    int32_t reserved[3];
 } rtdbs_params;
 
 /* Cumulative counters (src/dbscan/dbscan.cpp:145-212 keeps similar debug counters). */

@@ -1,6 +1,6 @@
 """Autotuner for a stream's launch configuration.
 
-Two knobs change how the engine works without changing its results:
+Three knobs change how the engine works without changing its results:
 - ``cell_mult`` (K): grid cells per Eps along each axis.  K = 2 scans the
   (2K+1)^d = 5^d cells of side Eps/2 around a point, which tests fewer pairs
   where cells are dense, but costs more cells, table lookups and work items
@@ -9,6 +9,10 @@ Two knobs change how the engine works without changing its results:
   shared queue at a time -- the work split between warps.  Small grabs balance
   uneven items; large ones keep consecutive cells on one warp and cost fewer
   queue atomics.
+- ``query_lanes``: the block shape of the count passes -- 16 lanes per expired
+  or new point (two points per warp, 16 per 256-thread block, their dependent
+  loads overlapping) or 32 (one point per warp, half the loop trips where
+  neighbourhoods are large).  Two cells per Eps always take 32.
 
 Streams are grouped into buckets by dimension, predicate, window size and
 density (mean points per occupied Eps-cell of a sample window).  For a
@@ -20,7 +24,7 @@ apart: `choose` times a single engine (its first window, then a few slides),
 `choose_batched` times pool rounds over up to 16 streams of each bucket
 together.  The default (one cell per Eps, 8 items per grab) is kept unless a
 candidate is at least 3% faster, so timing noise does not pick a
-configuration.
+configuration.  Candidates are (cell_mult, work_grab, query_lanes) triples.
 """
 from __future__ import annotations
 
@@ -34,8 +38,9 @@ import numpy as np
 
 from .engine import Engine, make_params
 
-# (cell_mult, work_grab); the first is the default
-CANDIDATES: Tuple[Tuple[int, int], ...] = ((1, 8), (1, 4), (1, 16), (2, 8), (2, 4), (2, 16))
+# (cell_mult, work_grab, query_lanes); the first is the default
+CANDIDATES: Tuple[Tuple[int, int, int], ...] = ((1, 8, 16), (1, 4, 16), (1, 16, 16), (1, 8, 32), (2, 8, 32),
+                                                (2, 4, 32), (2, 16, 32))
 MARGIN = 0.97           # a candidate replaces the default only when this much faster
 POOL_STREAMS = 16       # streams of a bucket timed together by choose_batched
 
@@ -61,10 +66,12 @@ def bucket_key(dim: int, window: int, precision: str, dens: float) -> str:
 
 
 class Autotuner:
-    """Picks (cell_mult, work_grab) per stream bucket.
+    """Picks (cell_mult, work_grab, query_lanes) per stream bucket.
 
-    `timer(points, dim, W, S, eps, min_pts, precision, cell_mult, work_grab)`
-    returns milliseconds per slide; the default times real slides on the GPU.
+    `timer(points, dim, W, S, eps, min_pts, precision, cell_mult, work_grab,
+    query_lanes)` returns milliseconds per slide; the default times real slides
+    on the GPU.  `pool_timer(streams, cell_mult, work_grab, query_lanes)` does
+    the same for pool rounds.
     """
 
     def __init__(self, cache_path: Optional[str] = None, device: int = 0, slides: int = 4,
@@ -88,13 +95,13 @@ class Autotuner:
 
     def choose(self, points: np.ndarray, dim: int, window: int, stride: int, eps: float, min_pts: int,
                precision: str = "fp64") -> dict:
-        """The bucket's configuration: {"cell_mult", "work_grab", "ms"}."""
+        """The bucket's configuration: {"cell_mult", "work_grab", "query_lanes", "ms"}."""
         key = bucket_key(dim, window, precision, density(points[:window], eps))
         hit = self.cache.get(key)
-        if hit is not None:
+        if hit is not None and "query_lanes" in hit:
             return hit
-        return self._tune(key, lambda km, grab: self.timer(points, dim, window, stride, eps, min_pts,
-                                                             precision, km, grab))
+        return self._tune(key, lambda km, grab, ql: self.timer(points, dim, window, stride, eps, min_pts,
+                                                                 precision, km, grab, ql))
 
     def choose_batched(self, streams) -> list:
         """Configurations for streams slid together in pool rounds.  `streams`
@@ -106,27 +113,27 @@ class Autotuner:
         for k, st in zip(keys, streams):
             groups.setdefault(k, []).append(st)
         for k, members in groups.items():
-            if k not in self.cache:
+            if "query_lanes" not in self.cache.get(k, {}):
                 sel = members[:POOL_STREAMS]
-                self._tune(k, lambda km, grab: self.pool_timer(sel, km, grab))
+                self._tune(k, lambda km, grab, ql: self.pool_timer(sel, km, grab, ql))
         return [self.cache[k] for k in keys]
 
     def _tune(self, key: str, run: Callable) -> dict:
         t0 = time.perf_counter()
         ms = {}
-        for km, grab in self.candidates:
+        for km, grab, ql in self.candidates:
             try:
-                ms[f"{km},{grab}"] = float(run(km, grab))
+                ms[f"{km},{grab},{ql}"] = float(run(km, grab, ql))
             except Exception:  # a configuration the stream cannot take is skipped
                 continue
         if not ms:
             raise RuntimeError(f"autotune: no candidate configuration ran for bucket {key}")
         best = min(ms, key=ms.get)
-        default = "{},{}".format(*self.candidates[0])
+        default = "{},{},{}".format(*self.candidates[0])
         if default in ms and ms[best] > MARGIN * ms[default]:
             best = default
-        km, grab = (int(x) for x in best.split(","))
-        self.cache[key] = {"cell_mult": km, "work_grab": grab, "ms": ms}
+        km, grab, ql = (int(x) for x in best.split(","))
+        self.cache[key] = {"cell_mult": km, "work_grab": grab, "query_lanes": ql, "ms": ms}
         self.tuned += 1
         self.tune_seconds += time.perf_counter() - t0
         self._save()
@@ -136,8 +143,8 @@ class Autotuner:
                precision: str = "fp64", **kw):
         """rtdbs_params of a stream with the tuned configuration."""
         c = self.choose(points, dim, window, stride, eps, min_pts, precision)
-        return make_params(dim, window, stride, eps, min_pts, precision=precision,
-                           cell_mult=c["cell_mult"], work_grab=c["work_grab"], **kw)
+        return make_params(dim, window, stride, eps, min_pts, precision=precision, cell_mult=c["cell_mult"],
+                           work_grab=c["work_grab"], query_lanes=c["query_lanes"], **kw)
 
     def _save(self) -> None:
         d = os.path.dirname(self.cache_path)
@@ -148,7 +155,8 @@ class Autotuner:
             json.dump(self.cache, f, indent=1, sort_keys=True)
         os.replace(tmp, self.cache_path)
 
-    def _time_on_gpu(self, points, dim, window, stride, eps, min_pts, precision, cell_mult, work_grab):
+    def _time_on_gpu(self, points, dim, window, stride, eps, min_pts, precision, cell_mult, work_grab,
+                     query_lanes):
         import torch
 
         need = window + (self.slides + 1) * stride
@@ -160,7 +168,8 @@ class Autotuner:
         torch.cuda.synchronize(dev)  # the copy is on torch's stream, the slides on s
         with torch.cuda.stream(s):
             with Engine(dim, window, stride, eps, min_pts, precision=precision, device=self.device,
-                        stream=s.cuda_stream, cell_mult=cell_mult, work_grab=work_grab) as eng:
+                        stream=s.cuda_stream, cell_mult=cell_mult, work_grab=work_grab,
+                        query_lanes=query_lanes) as eng:
                 eng.load_window(points[:window])
                 eng.slide_async(d[:stride])   # warm-up (and the graph capture)
                 a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -171,7 +180,7 @@ class Autotuner:
                 eng.sync()
                 return a.elapsed_time(b) / self.slides
 
-    def _time_pool_on_gpu(self, streams, cell_mult, work_grab, rounds: int = 3):
+    def _time_pool_on_gpu(self, streams, cell_mult, work_grab, query_lanes, rounds: int = 3):
         import torch
 
         from .engine import Pool
@@ -192,7 +201,8 @@ class Autotuner:
                 ids = []
                 for pts, dim, W, S, eps, mp, prec in streams:
                     sid = pool.add_stream(make_params(dim, W, S, eps, mp, precision=prec, device=self.device,
-                                                      cell_mult=cell_mult, work_grab=work_grab))
+                                                      cell_mult=cell_mult, work_grab=work_grab,
+                                                      query_lanes=query_lanes))
                     pool.load_window(sid, pts[:W])
                     ids.append(sid)
                 pool.slide(ids, packed[0])

@@ -34,7 +34,9 @@ void usage(const char* argv0) {
                  "         --fp64                   FP64 neighbour relation (default: FP32)\n"
                  "         --warmup <int>           untimed passes first (default 0)\n"
                  "         --labels <file>          write the last window's labels and ids\n"
-                 "         --cells-per-eps <1|2>    grid cells per Eps (default 1)\n",
+                 "         --cells-per-eps <1|2>    grid cells per Eps (default 1)\n"
+                 "         --query-lanes <16|32>    lanes per point in the count passes (default 16;\n"
+                 "                                  32 with two cells per Eps)\n",
                  argv0);
     std::exit(1);
 }
@@ -49,7 +51,7 @@ int die(const char* what, int rc) {
 int main(int argc, char** argv) {
     std::string file, labels_out;
     long long n = 0;
-    int W = 0, S = 0, K = 0, warmup = 0, precision = RTDBS_PREC_FP32, cell_mult = 1;
+    int W = 0, S = 0, K = 0, warmup = 0, precision = RTDBS_PREC_FP32, cell_mult = 1, query_lanes = 0;
     double R = 0.0;
     for (int i = 1; i < argc; ++i) {
         const std::string a(argv[i]);
@@ -68,6 +70,7 @@ int main(int argc, char** argv) {
         else if (a == "--warmup") warmup = std::atoi(next());
         else if (a == "--labels") labels_out = next();
         else if (a == "--cells-per-eps") cell_mult = std::atoi(next());
+        else if (a == "--query-lanes") query_lanes = std::atoi(next());
         else {
             std::fprintf(stderr, "Unknown option '%s'\n", a.c_str());
             usage(argv[0]);
@@ -106,6 +109,7 @@ int main(int argc, char** argv) {
     p.eps = R;
     p.precision = precision;
     p.cell_mult = cell_mult;
+    p.query_lanes = query_lanes;
     p.has_bbox = 1;
     for (int a = 0; a < 3; ++a) {
         p.bbox_min[a] = lo[a];

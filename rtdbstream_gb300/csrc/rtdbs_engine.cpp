@@ -376,6 +376,10 @@ int rtdbs_create(const rtdbs_params* params, void* cuda_stream, rtdbs_engine** o
         return fail(RTDBS_ERR_INVALID, "cell_mult must be 0 (default), 1 or 2 (got %d)", p.cell_mult);
     if (p.work_grab < 0 || p.work_grab > 64)
         return fail(RTDBS_ERR_INVALID, "work_grab must be 0 (default) or 1..64 (got %d)", p.work_grab);
+    if (p.query_lanes != 0 && p.query_lanes != 16 && p.query_lanes != 32)
+        return fail(RTDBS_ERR_INVALID, "query_lanes must be 0 (default), 16 or 32 (got %d)", p.query_lanes);
+    if (p.cell_mult == 2 && p.query_lanes == 16)
+        return fail(RTDBS_ERR_INVALID, "two cells per Eps need query_lanes 32 (or 0)");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(RTDBS_ERR_NO_DEVICE, "no CUDA device available");
@@ -402,6 +406,7 @@ int rtdbs_create(const rtdbs_params* params, void* cuda_stream, rtdbs_engine** o
     v.dim = p.dim;
     v.cell_mult = p.cell_mult > 0 ? p.cell_mult : 1;
     v.grab = p.work_grab > 0 ? p.work_grab : rtdbs::kBatch;
+    v.qlanes = p.query_lanes > 0 ? p.query_lanes : (v.cell_mult == 1 ? rtdbs::kQueryLanes : 32);
     v.W = p.window;
     v.S = p.stride;
     v.min_pts = p.min_pts;

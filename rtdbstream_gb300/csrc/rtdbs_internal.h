@@ -43,6 +43,8 @@ constexpr int kSortRun = 1024;     // words per radix-sort CTA (one per thread)
 constexpr int kBuildThreads = 512;
 constexpr int kClusterThreads = 256;
 constexpr int kBatch = 8;          // default work items a clustering warp takes at a time
+constexpr int kQueryLanes = 16;    // default lanes per query point in the count passes (one
+                                   // cell per Eps: two points per warp overlap their loads)
 constexpr int kMaxIter = 1 << 20;  // bound on every device-side retry loop
 constexpr int kListCap = 30;       // longest neighbour list kept (MinPts <= 32)
 
@@ -86,6 +88,7 @@ struct View {
     int dim;
     int cell_mult;              // K: cells per Eps along each axis (1 or 2)
     int grab;                   // work items a clustering warp takes from the queue at a time
+    int qlanes;                 // lanes per query point in the count passes (16 or 32)
     // parameters
     int W, S, min_pts, units;   // units = W / S
     int chunk;                  // C

@@ -631,11 +631,9 @@ __global__ void __launch_bounds__(kSortRun) k_runmerge(View v, int j, int c, int
 }
 
 // -1 on the count of every surviving neighbour of each expired point (old grid).
-// Lanes a count pass gives each query point: 16 (two points per warp, so
-// two queries' dependent loads overlap) with one cell per Eps; the 25 rows of
-// the two-cells-per-Eps stencil need the whole warp.
-constexpr int kQueryLanes = 16;
-__host__ __device__ constexpr int query_lanes(int k) { return k == 1 ? kQueryLanes : 32; }
+// G lanes scan one query point's neighbourhood (View::qlanes): 16 (two points
+// per warp, so two queries' dependent loads overlap) or 32; the 25 rows of the
+// two-cells-per-Eps stencil need the whole warp.
 
 struct StreamSmem {
     int rstart[8][kMaxRows], rpre[8][kMaxRows + 1];
@@ -646,10 +644,10 @@ struct StreamSmem {
     int nq;
 };
 
-template <int MODE, int DK>
-__device__ __forceinline__ void decr_body(const View& v, int j, int c, int bx, StreamSmem& sm) {
+template <int MODE, int DK, int G>
+__device__ __forceinline__ void decr_g(const View& v, int j, int c, int bx, StreamSmem& sm) {
     constexpr int DIM = DK & 3, K = (DK >> 2) + 1;  // dimension, cells per Eps
-    constexpr int G = query_lanes(K), kPerWarp = 32 / G;
+    constexpr int kPerWarp = 32 / G;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int grp = lane / G, gl = lane % G;
     const int gw = (bx * blockDim.x + threadIdx.x) >> 5;
@@ -697,6 +695,19 @@ __device__ __forceinline__ void decr_body(const View& v, int j, int c, int bx, S
         }
     }
     flush_stats(v, tally, 0, lane);
+}
+
+// The count passes' lane group, chosen per stream at run time (uniform per
+// launch): 16 or 32 lanes with one cell per Eps, 32 with two.
+template <int MODE, int DK>
+__device__ __forceinline__ void decr_body(const View& v, int j, int c, int bx, StreamSmem& sm) {
+    if constexpr ((DK >> 2) == 0) {
+        if (v.qlanes == 16) {
+            decr_g<MODE, DK, 16>(v, j, c, bx, sm);
+            return;
+        }
+    }
+    decr_g<MODE, DK, 32>(v, j, c, bx, sm);
 }
 
 template <int MODE, int DK>
@@ -1007,10 +1018,10 @@ __global__ void __launch_bounds__(kBuildThreads) k_build(View v) {
 }
 
 // Full count of each new point and +1 on every older neighbour (new grid).
-template <int MODE, int DK>
-__device__ __forceinline__ void incr_body(const View& v, int j, int c, int init, int bx, StreamSmem& sm) {
+template <int MODE, int DK, int G>
+__device__ __forceinline__ void incr_g(const View& v, int j, int c, int init, int bx, StreamSmem& sm) {
     constexpr int DIM = DK & 3, K = (DK >> 2) + 1;  // dimension, cells per Eps
-    constexpr int G = query_lanes(K), kPerWarp = 32 / G;
+    constexpr int kPerWarp = 32 / G;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int grp = lane / G, gl = lane % G;
     const int gw = (bx * blockDim.x + threadIdx.x) >> 5;
@@ -1077,6 +1088,17 @@ __device__ __forceinline__ void incr_body(const View& v, int j, int c, int init,
             err = kErrChunk;
     }
     flush_stats(v, tally, err, lane);
+}
+
+template <int MODE, int DK>
+__device__ __forceinline__ void incr_body(const View& v, int j, int c, int init, int bx, StreamSmem& sm) {
+    if constexpr ((DK >> 2) == 0) {
+        if (v.qlanes == 16) {
+            incr_g<MODE, DK, 16>(v, j, c, init, bx, sm);
+            return;
+        }
+    }
+    incr_g<MODE, DK, 32>(v, j, c, init, bx, sm);
 }
 
 template <int MODE, int DK>
@@ -1659,7 +1681,7 @@ cudaError_t configure_kernels() {
 
 cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, int init,
                          int stg_off, int advance, cudaStream_t s) {
-    const int warp_blocks = (c * query_lanes(v.cell_mult) + 255) / 256;  // count passes
+    const int warp_blocks = (c * v.qlanes + 255) / 256;  // count passes
     switch (phase) {
         case kPhaseIngest:
             k_ingest<<<(c + 255) / 256, 256, 0, s>>>(v, j, c, init, stg_off);
@@ -1764,7 +1786,7 @@ int batch_blocks(int phase, const View& v, int c) {
         case kBatchSort:
         case kBatchRunmerge: return 2 * runs;
         case kBatchDecrement:
-        case kBatchIncrement: return (c * query_lanes(v.cell_mult) + 255) / 256;
+        case kBatchIncrement: return (c * v.qlanes + 255) / 256;
         case kBatchMerge: return (v.W + kMergeTile - 1) / kMergeTile;
         case kBatchBuild: return (v.W + kBuildThreads - 1) / kBuildThreads;
         case kBatchDamage: return v.list_cap >= 0 ? max(1, min(1024, (v.W + 2047) / 2048)) : 0;

@@ -163,6 +163,7 @@ extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int
     v.dim = dim;
     v.cell_mult = 1;
     v.grab = rtdbs::kBatch;
+    v.qlanes = rtdbs::kQueryLanes;
     v.W = n;
     v.S = n;
     v.units = 1;

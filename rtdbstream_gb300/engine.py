@@ -46,7 +46,7 @@ class Params(ctypes.Structure):
                 ("has_bbox", ctypes.c_int32), ("bbox_min", ctypes.c_float * 3),
                 ("bbox_max", ctypes.c_float * 3), ("device", ctypes.c_int32),
                 ("flags", ctypes.c_int32), ("cell_mult", ctypes.c_int32), ("work_grab", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 4)]
+                ("query_lanes", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 
 
 class Stats(ctypes.Structure):
@@ -162,10 +162,12 @@ class Engine:
 
     def __init__(self, dim: int, window_size: int, stride_size: int, radius: float, min_pts: int,
                  precision: str = "fp64", bbox: Optional[Tuple] = None, device: int = 0,
-                 use_graph: bool = True, stream: int = 0, cell_mult: int = 1, work_grab: int = 0):
+                 use_graph: bool = True, stream: int = 0, cell_mult: int = 1, work_grab: int = 0,
+                 query_lanes: int = 0):
         self._lib = load_library()
         p = make_params(dim, window_size, stride_size, radius, min_pts, precision=precision, bbox=bbox,
-                        device=device, use_graph=use_graph, cell_mult=cell_mult, work_grab=work_grab)
+                        device=device, use_graph=use_graph, cell_mult=cell_mult, work_grab=work_grab,
+                        query_lanes=query_lanes)
         self.params = p
         self.dim, self.window_size, self.stride_size = p.dim, p.window, p.stride
         self.radius, self.min_pts = p.eps, p.min_pts
@@ -257,9 +259,12 @@ class Engine:
 
 def make_params(dim: int, window_size: int, stride_size: int, radius: float, min_pts: int,
                 precision: str = "fp64", bbox: Optional[Tuple] = None, device: int = 0,
-                use_graph: bool = True, cell_mult: int = 1, work_grab: int = 0) -> Params:
+                use_graph: bool = True, cell_mult: int = 1, work_grab: int = 0,
+                query_lanes: int = 0) -> Params:
     """rtdbs_params for one stream; cell_mult = grid cells per Eps (1 or 2),
-    work_grab = work items per queue grab of the clustering warps (0: 8)."""
+    work_grab = work items per queue grab of the clustering warps (0: 8),
+    query_lanes = lanes per query point in the count passes (0: 16 with one
+    cell per Eps, 32 with two; 16 or 32)."""
     L = load_library()
     p = Params()
     _check(L.rtdbs_params_init(ctypes.byref(p)))
@@ -270,6 +275,7 @@ def make_params(dim: int, window_size: int, stride_size: int, radius: float, min
     p.flags = 0 if use_graph else FLAG_NO_GRAPH
     p.cell_mult = int(cell_mult)
     p.work_grab = int(work_grab)
+    p.query_lanes = int(query_lanes)
     if bbox is not None:
         lo, hi = bbox
         p.has_bbox = 1

@@ -56,12 +56,16 @@ def test_params_init_defaults(lib):
 @pytest.mark.parametrize("field,value", [("dim", 4), ("dim", 0), ("stride", 7), ("eps", 0.0),
                                          ("eps", float("nan")), ("precision", 9), ("stride", 0),
                                          ("cell_mult", 3), ("cell_mult", -1), ("work_grab", 65),
-                                         ("work_grab", -2)])
+                                         ("work_grab", -2), ("query_lanes", 8), ("query_lanes", 64),
+                                         ("query_lanes", -16), ("two_cells_16_lanes", None)])
 def test_invalid_params_rejected_before_device(lib, field, value):
     p = E.Params()
     lib.rtdbs_params_init(ctypes.byref(p))
     p.dim, p.window, p.stride, p.min_pts, p.eps = 2, 100, 10, 4, 0.5
-    setattr(p, field, value)
+    if field == "two_cells_16_lanes":  # the two-cells-per-Eps stencil needs the whole warp
+        p.cell_mult, p.query_lanes = 2, 16
+    else:
+        setattr(p, field, value)
     h = ctypes.c_void_p()
     rc = lib.rtdbs_create(ctypes.byref(p), None, ctypes.byref(h))
     assert rc == E.RTDBS_ERR_INVALID

@@ -11,11 +11,11 @@ from rtdbstream_gb300 import workloads as wl
 
 
 def fake_timer(table, calls):
-    def timer(points, dim, W, S, eps, mp, prec, km, grab):
-        calls.append((km, grab))
-        if (km, grab) not in table:
+    def timer(points, dim, W, S, eps, mp, prec, km, grab, ql):
+        calls.append((km, grab, ql))
+        if (km, grab, ql) not in table:
             raise RuntimeError("configuration not available")
-        return table[(km, grab)]
+        return table[(km, grab, ql)]
     return timer
 
 
@@ -30,12 +30,12 @@ def test_density_and_buckets():
 
 def test_picks_fastest_and_caches(tmp_path):
     cache = tmp_path / "tune.json"
-    table = {(1, 8): 2.0, (1, 4): 1.5, (2, 8): 1.2, (2, 4): 3.0}   # (1, 16), (2, 16) unavailable
+    table = {(1, 8, 16): 2.0, (1, 4, 16): 1.5, (1, 8, 32): 1.9, (2, 8, 32): 1.2, (2, 4, 32): 3.0}  # others unavailable
     calls = []
     tuner = AT.Autotuner(cache_path=str(cache), timer=fake_timer(table, calls))
     pts = wl.gaussian_mixture(12_000, dim=2, k=4, box=20.0, seed=2)
     c = tuner.choose(pts, 2, 10_000, 500, 0.5, 5)
-    assert (c["cell_mult"], c["work_grab"]) == (2, 8)
+    assert (c["cell_mult"], c["work_grab"], c["query_lanes"]) == (2, 8, 32)
     assert len(calls) == len(AT.CANDIDATES) and tuner.tuned == 1
     # another stream of the same bucket: no timing
     pts2 = wl.gaussian_mixture(12_000, dim=2, k=4, box=20.0, seed=3)
@@ -47,6 +47,19 @@ def test_picks_fastest_and_caches(tmp_path):
     calls.clear()
     again = AT.Autotuner(cache_path=str(cache), timer=fake_timer(table, calls))
     assert again.choose(pts, 2, 10_000, 500, 0.5, 5)["work_grab"] == 8 and not calls
+
+
+def test_cache_without_block_shape_is_retuned(tmp_path):
+    """A cache written before the block-shape knob (no query_lanes) is timed
+    again for the buckets it is asked about."""
+    cache = tmp_path / "old.json"
+    pts = wl.gaussian_mixture(12_000, dim=2, k=4, box=20.0, seed=2)
+    key = AT.bucket_key(2, 10_000, "fp64", AT.density(pts[:10_000], 0.5))
+    cache.write_text(json.dumps({key: {"cell_mult": 2, "work_grab": 4, "ms": {"2,4": 1.0}}}))
+    calls = []
+    tuner = AT.Autotuner(cache_path=str(cache), timer=fake_timer({(1, 8, 32): 1.0, (1, 8, 16): 2.0}, calls))
+    c = tuner.choose(pts, 2, 10_000, 500, 0.5, 5)
+    assert calls and (c["cell_mult"], c["work_grab"], c["query_lanes"]) == (1, 8, 32)
 
 
 def test_no_candidate_raises(tmp_path):
@@ -73,9 +86,10 @@ def test_tuned_streams_match_oracle(tmp_path):
     ]
     for pts, dim, W, S, eps, mp in cases:
         c = tuner.choose(pts, dim, W, S, eps, mp)
-        assert (c["cell_mult"], c["work_grab"]) in AT.CANDIDATES
+        assert (c["cell_mult"], c["work_grab"], c["query_lanes"]) in AT.CANDIDATES
         assert len(c["ms"]) == len(AT.CANDIDATES) and all(v > 0 for v in c["ms"].values())
-        with Engine(dim, W, S, eps, mp, cell_mult=c["cell_mult"], work_grab=c["work_grab"]) as eng:
+        with Engine(dim, W, S, eps, mp, cell_mult=c["cell_mult"], work_grab=c["work_grab"],
+                    query_lanes=c["query_lanes"]) as eng:
             eng.load_window(pts[:W])
             for k in range(2):
                 lab, cid = eng.slide(pts[W + k * S: W + (k + 1) * S])
@@ -85,15 +99,16 @@ def test_tuned_streams_match_oracle(tmp_path):
     # pool rounds: every candidate timed on the bucket's streams together
     got = tuner.choose_batched([(pts, dim, W, S, eps, mp, "fp64") for pts, dim, W, S, eps, mp in cases])
     for c in got:
-        assert (c["cell_mult"], c["work_grab"]) in AT.CANDIDATES and len(c["ms"]) == len(AT.CANDIDATES)
+        assert (c["cell_mult"], c["work_grab"], c["query_lanes"]) in AT.CANDIDATES
+        assert len(c["ms"]) == len(AT.CANDIDATES)
 
 
 def test_batched_tuning_per_bucket_and_margin(tmp_path):
     calls = []
 
-    def pool_timer(streams, km, grab):
+    def pool_timer(streams, km, grab, ql):
         calls.append((len(streams), km, grab))
-        return {(1, 8): 1.0, (1, 4): 0.99, (2, 8): 0.5}.get((km, grab), 2.0)
+        return {(1, 8, 16): 1.0, (1, 4, 16): 0.99, (2, 8, 32): 0.5}.get((km, grab, ql), 2.0)
 
     tuner = AT.Autotuner(cache_path=str(tmp_path / "t.json"), timer=fake_timer({}, []), pool_timer=pool_timer)
     dense = wl.gaussian_mixture(6_000, dim=2, k=2, box=5.0, sigma=0.2, seed=7)
@@ -106,6 +121,6 @@ def test_batched_tuning_per_bucket_and_margin(tmp_path):
     assert (out[0]["cell_mult"], out[0]["work_grab"]) == (2, 8)       # 2x faster: taken
     # (1, 4) is only 1% faster than the default: the default is kept
     tuner2 = AT.Autotuner(cache_path=str(tmp_path / "t2.json"), timer=fake_timer({}, []),
-                          pool_timer=lambda st, km, grab: {(1, 8): 1.0, (1, 4): 0.99}.get((km, grab), 2.0))
-    assert (tuner2.choose_batched(streams[:1])[0]["cell_mult"], tuner2.choose_batched(streams[:1])[0]["work_grab"]) \
-        == (1, 8)
+                          pool_timer=lambda st, km, grab, ql: {(1, 8, 16): 1.0, (1, 4, 16): 0.99}.get((km, grab, ql), 2.0))
+    c2 = tuner2.choose_batched(streams[:1])[0]
+    assert (c2["cell_mult"], c2["work_grab"], c2["query_lanes"]) == (1, 8, 16)

@@ -13,8 +13,8 @@ from rtdbstream_gb300 import workloads as wl
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("cells_per_eps", [1, 2])
-def test_cli_tao_stream(tmp_path, cells_per_eps):
+@pytest.mark.parametrize("cells_per_eps,query_lanes", [(1, 16), (2, 32), (1, 32)])
+def test_cli_tao_stream(tmp_path, cells_per_eps, query_lanes):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no GPU")
@@ -26,7 +26,8 @@ def test_cli_tao_stream(tmp_path, cells_per_eps):
     out = tmp_path / "labels.bin"
     W, S, K, R = 1_000, 250, 5, 1.0
     r = subprocess.run([rbuild.CLI, "-f", str(path), "-n", "3000", "-W", str(W), "-S", str(S), "-K", str(K),
-                        "-R", str(R), "--labels", str(out), "--cells-per-eps", str(cells_per_eps)],
+                        "-R", str(R), "--labels", str(out), "--cells-per-eps", str(cells_per_eps),
+                        "--query-lanes", str(query_lanes)],
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert "[Time] total:" in r.stdout

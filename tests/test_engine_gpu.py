@@ -27,9 +27,10 @@ def _built():
         pytest.skip("no GPU")
 
 
-def run_stream(points, W, S, eps, mp, n_slides, precision="fp64", use_graph=True, bbox=None, cell_mult=1):
+def run_stream(points, W, S, eps, mp, n_slides, precision="fp64", use_graph=True, bbox=None, cell_mult=1,
+               query_lanes=0):
     eng = Engine(points.shape[1], W, S, eps, mp, precision=precision, use_graph=use_graph, bbox=bbox,
-                 cell_mult=cell_mult)
+                 cell_mult=cell_mult, query_lanes=query_lanes)
     eng.load_window(points[:W])
     labs, cids, nns = [], [], []
     for k in range(n_slides):
@@ -401,3 +402,20 @@ def test_extreme_eps_match_oracle(eps, precision, cell_mult):
     assert_same(got[:3], exp, f"eps {eps}/{precision}/K{cell_mult}")
     if eps > 1.0:
         assert np.all(got[1] == 0)  # one cluster of cores
+
+
+# The count passes' block shape: a whole warp per expired or new point
+# instead of a 16-lane half (one cell per Eps).
+LANES_CASES = [c for c in CASES if c[0] in ("mix2d_W10k_S1k", "walk3d_W60k_S6k", "band3d_W20k_S2k", "stk1d_W8k_S2k",
+                                            "big_stride_W40k_S20k", "mix3d_mp32_W12k")] + \
+    [c for c in STEADY_CASES if c[0] in ("mix2d_W2k_S200", "S1_W16_2d")]
+
+
+@pytest.mark.parametrize("name,gen,W,S,eps,mp,slides", LANES_CASES, ids=[c[0] for c in LANES_CASES])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_count_passes_with_whole_warp_queries(name, gen, W, S, eps, mp, slides, precision):
+    pts = gen()
+    got = run_stream(pts, W, S, eps, mp, slides, precision=precision, query_lanes=32)
+    mode = O.MODE_FP64 if precision == "fp64" else O.MODE_FP32
+    exp = O.stream(pts, W, S, eps, mp, mode, first_slide=1, n_out=slides)
+    assert_same(got[:3], exp, f"{name}/{precision}/32 lanes")

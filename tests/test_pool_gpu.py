@@ -154,18 +154,23 @@ def test_pool_rejects_unloaded_and_duplicate_streams():
 
 
 def test_pool_mixes_cell_multipliers():
-    """Streams with one and two cells per Eps in one pool (separate launch
-    groups) equal the same streams alone and the oracle."""
-    specs = [(2, 4_000, 400, 0.5, 5, 1), (2, 4_000, 400, 0.5, 5, 2), (3, 6_000, 600, 0.8, 6, 2),
-             (3, 6_000, 600, 0.8, 6, 1)]
+    """Streams with one and two cells per Eps (separate launch groups) and
+    with 16 or 32 lanes per count query (one group, a block shape per stream)
+    in one pool equal the same streams alone and the oracle."""
+    specs = [(2, 4_000, 400, 0.5, 5, (1, 0)), (2, 4_000, 400, 0.5, 5, (2, 0)), (3, 6_000, 600, 0.8, 6, (2, 0)),
+             (3, 6_000, 600, 0.8, 6, (1, 0)), (2, 4_000, 400, 0.5, 5, (1, 32)), (3, 6_000, 600, 0.8, 6, (1, 32))]
     data = [wl.gaussian_mixture(W + ROUNDS * S, dim=dim, k=6, box=20.0, seed=300 + i)
             for i, (dim, W, S, eps, mp, km) in enumerate(specs)]
+
+    def shape(km):  # (cells per Eps, lanes per count query)
+        return {"cell_mult": km[0], "query_lanes": km[1]}
+
     import torch
 
     with Pool() as pool:
         ids = []
         for (dim, W, S, eps, mp, km), d in zip(specs, data):
-            sid = pool.add_stream(make_params(dim, W, S, eps, mp, cell_mult=km))
+            sid = pool.add_stream(make_params(dim, W, S, eps, mp, **shape(km)))
             pool.load_window(sid, d[:W])
             ids.append(sid)
         for k in range(ROUNDS):
@@ -174,7 +179,7 @@ def test_pool_mixes_cell_multipliers():
             pool.slide(ids, buf)
         for sid, (dim, W, S, eps, mp, km), d in zip(ids, specs, data):
             lab, cid = pool.outputs(sid)
-            with Engine(dim, W, S, eps, mp, cell_mult=km) as eng:
+            with Engine(dim, W, S, eps, mp, **shape(km)) as eng:
                 eng.load_window(d[:W])
                 for k in range(ROUNDS):
                     elab, ecid = eng.slide(d[W + k * S: W + (k + 1) * S])
