@@ -132,10 +132,10 @@ struct Tally {
     unsigned rechecks = 0;
 };
 
+// The decision on d = sqdist32(a, b).
 template <int MODE, int DIM>
-__device__ __forceinline__ bool is_nbr(const View& v, const float4& a, const float4& b, Tally& t) {
+__device__ __forceinline__ bool nbr_decide(const View& v, float d, const float4& a, const float4& b, Tally& t) {
     ++t.tests;
-    const float d = sqdist32<DIM>(a, b);
     if (MODE == kPrecFp32) return d < v.r2f;
     if (v.filter_ok) {
         if (d < v.lo) return true;
@@ -143,6 +143,48 @@ __device__ __forceinline__ bool is_nbr(const View& v, const float4& a, const flo
     }
     ++t.rechecks;
     return sqdist64<DIM>(a, b) < v.E;
+}
+
+template <int MODE, int DIM>
+__device__ __forceinline__ bool is_nbr(const View& v, const float4& a, const float4& b, Tally& t) {
+    return nbr_decide<MODE, DIM>(v, sqdist32<DIM>(a, b), a, b, t);
+}
+
+// sqdist32(a, b0) and sqdist32(a, b1) at once: the differences and squares
+// with paired FP32 instructions (Blackwell f32x2, each half an IEEE single
+// operation rounded to nearest), the sums in scalar, in the same order as
+// sqdist32, so both results are bit-identical to it.  (Paired sums are not
+// used: the paired multiply-then-add did not round like the two separate
+// scalar operations.)
+__device__ __forceinline__ unsigned long long pack2(float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+
+__device__ __forceinline__ void sq_diff2(float a, float b0, float b1, float& s0, float& s1) {
+    unsigned long long t, m;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t) : "l"(pack2(a, a)), "l"(pack2(b0, b1)));
+    asm("mul.rn.f32x2 %0, %1, %1;" : "=l"(m) : "l"(t));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(s0), "=f"(s1) : "l"(m));
+}
+
+template <int DIM>
+__device__ __forceinline__ void sqdist32x2(const float4& a, const float4& b0, const float4& b1, float& d0,
+                                           float& d1) {
+    sq_diff2(a.x, b0.x, b1.x, d0, d1);
+    if (DIM > 1) {
+        float y0, y1;
+        sq_diff2(a.y, b0.y, b1.y, y0, y1);
+        d0 = __fadd_rn(d0, y0);
+        d1 = __fadd_rn(d1, y1);
+    }
+    if (DIM > 2) {
+        float z0, z1;
+        sq_diff2(a.z, b0.z, b1.z, z0, z1);
+        d0 = __fadd_rn(d0, z0);
+        d1 = __fadd_rn(d1, z1);
+    }
 }
 
 // ---------------------------------------------------------------- cell table
@@ -684,14 +726,25 @@ __device__ __forceinline__ void decr_g(const View& v, int j, int c, int bx, Stre
     const int xs = slot_of(xp);
     Tally tally;
     int r = 0;
-    for (int idx = gl; idx < total; idx += G) {
-        const int pos = stream_pos(idx, r, rstart, rpre);
-        const float4 q = spt[pos];
-        const int cnt = scnt[pos];  // counts only fall here: >= MinPts means no list kept
-        const int qs = slot_of(q);
-        if ((qs < el || qs >= el + c) && is_nbr<MODE, DIM>(v, xp, q, tally)) {
-            atomicSub(&scnt[pos], 1);
-            if (lists && cnt < v.min_pts && v.ntrack[qs] == 1) list_remove(v, qs, xs);
+    // Two candidates per lane and trip (idx and idx + G): their loads are in
+    // flight together and one paired distance evaluation serves both.
+    for (int idx = gl; idx < total; idx += 2 * G) {
+        const bool two = idx + G < total;
+        const int pos0 = stream_pos(idx, r, rstart, rpre);
+        const int pos1 = two ? stream_pos(idx + G, r, rstart, rpre) : pos0;
+        const float4 q0 = spt[pos0], q1 = spt[pos1];
+        // counts only fall here: >= MinPts means no list kept
+        const int cnt0 = scnt[pos0], cnt1 = scnt[pos1];
+        const int qs0 = slot_of(q0), qs1 = slot_of(q1);
+        float d0, d1;
+        sqdist32x2<DIM>(xp, q0, q1, d0, d1);
+        if ((qs0 < el || qs0 >= el + c) && nbr_decide<MODE, DIM>(v, d0, xp, q0, tally)) {
+            atomicSub(&scnt[pos0], 1);
+            if (lists && cnt0 < v.min_pts && v.ntrack[qs0] == 1) list_remove(v, qs0, xs);
+        }
+        if (two && (qs1 < el || qs1 >= el + c) && nbr_decide<MODE, DIM>(v, d1, xp, q1, tally)) {
+            atomicSub(&scnt[pos1], 1);
+            if (lists && cnt1 < v.min_pts && v.ntrack[qs1] == 1) list_remove(v, qs1, xs);
         }
     }
     flush_stats(v, tally, 0, lane);
@@ -1051,28 +1104,45 @@ __device__ __forceinline__ void incr_g(const View& v, int j, int c, int init, in
     int* nbuf = sm.gnbuf[wib][grp];
     Tally tally;
     int count = 0, mypos = -1, r = 0, nfound = 0;
-    for (int base = 0; base < tmax; base += G) {
+    // Two candidates per lane and trip (idx and idx + G), as in the decrement.
+    for (int base = 0; base < tmax; base += 2 * G) {
         const int idx = base + gl;
-        bool nb = false;
-        int qs = -1;
-        if (idx < total) {
-            const int pos = stream_pos(idx, r, rstart, rpre);
-            const float4 q = spt[pos];
-            const int cnt = scnt[pos];  // counts only rise here: >= MinPts means no list kept
-            qs = slot_of(q);
-            if (qs == aslot) {
+        const bool h0 = idx < total, h1 = idx + G < total;
+        int pos[2] = {0, 0}, cnt[2] = {0, 0}, qs[2] = {-1, -1};
+        float4 q[2] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
+        if (h0) {
+            pos[0] = stream_pos(idx, r, rstart, rpre);
+            q[0] = spt[pos[0]];
+            cnt[0] = scnt[pos[0]];  // counts only rise here: >= MinPts means no list kept
+        }
+        if (h1) {
+            pos[1] = stream_pos(idx + G, r, rstart, rpre);
+            q[1] = spt[pos[1]];
+            cnt[1] = scnt[pos[1]];
+        }
+        float d[2];
+        sqdist32x2<DIM>(ap, q[0], q[1], d[0], d[1]);
+        bool nb[2] = {false, false};
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            if (!(u == 0 ? h0 : h1)) continue;
+            qs[u] = slot_of(q[u]);
+            if (qs[u] == aslot) {
                 ++count;
-                mypos = pos;
-            } else if (is_nbr<MODE, DIM>(v, ap, q, tally)) {
+                mypos = pos[u];
+            } else if (nbr_decide<MODE, DIM>(v, d[u], ap, q[u], tally)) {
                 ++count;
-                nb = true;
-                if (qs < el || qs >= el + c) {
-                    atomicAdd(&scnt[pos], 1);
-                    if (lists && cnt < v.min_pts && v.ntrack[qs] == 1) list_append(v, qs, aslot);
+                nb[u] = true;
+                if (qs[u] < el || qs[u] >= el + c) {
+                    atomicAdd(&scnt[pos[u]], 1);
+                    if (lists && cnt[u] < v.min_pts && v.ntrack[qs[u]] == 1) list_append(v, qs[u], aslot);
                 }
             }
         }
-        if (lists) nfound = list_collect<G>(nb, qs, nfound, v.list_cap, nbuf, lane);
+        if (lists) {
+            nfound = list_collect<G>(nb[0], qs[0], nfound, v.list_cap, nbuf, lane);
+            nfound = list_collect<G>(nb[1], qs[1], nfound, v.list_cap, nbuf, lane);
+        }
     }
     if (lists) list_store<G>(v, aslot, nfound, nbuf, lane, has);
 #pragma unroll
