@@ -9,9 +9,10 @@
 //     k_sort    LSD radix sort of the new and of the expired (cell key, slot)
 //               words in runs of 1024, one CTA per run, then k_runmerge
 //               ranks the runs into one list (reference: sortByCellIdAndOrder,
-//               src/dbscan/thrust_helper.cu:21-29)
+//               src/dbscan/thrust_helper.cu:21-29); expired words whose order
+//               was kept from their arrival are gathered instead of sorted
 //     k_decr    exact -1 on the neighbour counts of every survivor within Eps
-//               of an expired point, on the old grid
+//               of an expired point, on the old grid, beside the sort
 //     k_merge   old sorted window minus expired plus new, one pass, merge-path
 //               tiles (reference: merge_by_cell_id_and_idx,
 //               src/dbscan/thrust_helper.cu:31-51)
@@ -33,8 +34,10 @@
 // Neighbour predicate: a warp holds 32 candidates in lanes (coalesced float4
 // loads of the cell-sorted window) and tests them against home points
 // broadcast by shuffle.  Squared distances use explicitly rounded IEEE
-// operations (no FMA contraction), so FP32 mode is bit-identical to the
-// reference's CPU checker (src/dbscan/util.cpp:308-316).
+// operations (no FMA contraction; the count passes evaluate two candidates'
+// differences and squares with paired FP32 instructions, each half rounded
+// the same way), so FP32 mode is bit-identical to the reference's CPU checker
+// (src/dbscan/util.cpp:308-316).
 #include "rtdbs_internal.h"
 
 #include <atomic>
