@@ -124,3 +124,20 @@ def test_batched_tuning_per_bucket_and_margin(tmp_path):
                           pool_timer=lambda st, km, grab, ql: {(1, 8, 16): 1.0, (1, 4, 16): 0.99}.get((km, grab, ql), 2.0))
     c2 = tuner2.choose_batched(streams[:1])[0]
     assert (c2["cell_mult"], c2["work_grab"], c2["query_lanes"]) == (1, 8, 16)
+
+
+def test_every_candidate_is_a_valid_configuration():
+    """The engine's parameter checks (which run before any device call) accept
+    every candidate, so a tuned choice can always be created."""
+    import ctypes
+
+    from rtdbstream_gb300 import engine as E
+
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present: creation would succeed, not stop at the device check")
+    lib = E.load_library()
+    for km, grab, ql in AT.CANDIDATES:
+        p = E.make_params(3, 10_000, 500, 0.5, 5, cell_mult=km, work_grab=grab, query_lanes=ql)
+        h = ctypes.c_void_p()
+        assert lib.rtdbs_create(ctypes.byref(p), None, ctypes.byref(h)) == E.RTDBS_ERR_NO_DEVICE, (km, grab, ql)
