@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define RTDBS_ABI_VERSION 1
+#define RTDBS_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define RTDBS_API __attribute__((visibility("default")))
@@ -116,11 +116,21 @@ typedef struct rtdbs_stats {
     int32_t launches_per_slide; /* kernels launched by one slide */
     int32_t chunks_per_slide;   /* grid-update chunks per slide (ceil(S / 16384)) */
     int64_t dist_tests;         /* distance tests evaluated, cumulative (the reference's
-                                   DEBUG_INFO num_dist_calculations, src/dbscan/dbscan.cpp:145-212) */
+                                   DEBUG_INFO num_dist_calculations, src/dbscan/dbscan.cpp:145-212);
+                                   query_tests + cluster_tests */
     int64_t reused_cores;       /* cores that started the last clustering in a component
                                    kept from the previous slide (no counterpart in the
                                    reference, which re-clusters every slide) */
-    int64_t reserved[1];
+    /* The reference's DEBUG_INFO ray counters (print_rt_info,
+     * src/dbscan/dbscan.cpp:145-178), cumulative: */
+    int64_t query_tests;        /* count passes (core identification): distance tests, the
+                                   intersection tests of its core rays (ray_intersections) */
+    int64_t query_hits;         /* ... that found a neighbour (ray_primitive_hits) */
+    int64_t cluster_tests;      /* clustering scans: distance tests (ray_intersections_cluster) */
+    int64_t cluster_hits;       /* ... that found a neighbour (ray_primitive_hits_cluster) */
+    int32_t max_query_tests;    /* most distance tests of one count query (max_ray_intersections) */
+    int32_t reserved0;
+    int64_t reserved[3];
 } rtdbs_stats;
 
 /* Per-phase device time of one profiled slide, in milliseconds (the

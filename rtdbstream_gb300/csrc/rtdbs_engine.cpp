@@ -574,7 +574,14 @@ int rtdbs_get_stats(rtdbs_engine* e, rtdbs_stats* s) {
     std::memset(s, 0, sizeof(*s));
     s->slides = e->h_ctl->slide;
     s->band_rechecks = (int64_t)e->h_ctl->band_rechecks;
-    for (int k = 0; k < 8; ++k) s->dist_tests += (int64_t)e->h_ctl->dist_tests[k];
+    for (int k = 0; k < 8; ++k) {
+        s->query_tests += (int64_t)e->h_ctl->ptests[0][k];
+        s->query_hits += (int64_t)e->h_ctl->phits[0][k];
+        s->cluster_tests += (int64_t)e->h_ctl->ptests[1][k];
+        s->cluster_hits += (int64_t)e->h_ctl->phits[1][k];
+        s->max_query_tests = std::max(s->max_query_tests, e->h_ctl->qmax[k]);
+    }
+    s->dist_tests = s->query_tests + s->cluster_tests;
     s->reused_cores = e->h_ctl->last_reused;
     s->cells = e->h_ctl->ncells;
     s->work_items = e->h_ctl->nitems;

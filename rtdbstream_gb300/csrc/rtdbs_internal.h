@@ -70,7 +70,11 @@ struct Ctl {
     int union_next;            // next work item handed out by k_union
     int label_next;            // next work item handed out by k_label
     unsigned long long band_rechecks;
-    unsigned long long dist_tests[8];  // distance tests evaluated, spread over 8 counters
+    // counters of the reference's debug build (src/dbscan/dbscan.cpp:145-212):
+    // [0] count passes (core identification), [1] clustering scans; spread over 8
+    unsigned long long ptests[2][8];   // distance tests
+    unsigned long long phits[2][8];    // ... that found a neighbour
+    int qmax[8];                       // most distance tests of one count query
     int reused;                // cores that joined a reused component this slide
     int reuse_skip;            // slides left without forest reuse (it paid off too little)
     long long last_reused;     // `reused` of the last clustering

@@ -129,23 +129,31 @@ __device__ __forceinline__ double sqdist64(const float4& a, const float4& b) {
 // d32 < r2f.  FP64 mode: d32 < lo and d32 >= hi are decided by the float
 // value (the band [lo, hi) around Eps^2 bounds the float evaluation's
 // rounding error, see oracle_band); everything else in double.
-// Per-thread counters: distance tests, and those re-decided in FP64.
+// Per-thread counters: distance tests, those re-decided in FP64, and those
+// that found a neighbour.
 struct Tally {
     unsigned tests = 0;
     unsigned rechecks = 0;
+    unsigned hits = 0;
 };
 
 // The decision on d = sqdist32(a, b).
 template <int MODE, int DIM>
 __device__ __forceinline__ bool nbr_decide(const View& v, float d, const float4& a, const float4& b, Tally& t) {
     ++t.tests;
-    if (MODE == kPrecFp32) return d < v.r2f;
-    if (v.filter_ok) {
-        if (d < v.lo) return true;
-        if (d >= v.hi) return false;
+    bool nb;
+    if (MODE == kPrecFp32) {
+        nb = d < v.r2f;
+    } else if (v.filter_ok && d < v.lo) {
+        nb = true;
+    } else if (v.filter_ok && d >= v.hi) {
+        nb = false;
+    } else {
+        ++t.rechecks;
+        nb = sqdist64<DIM>(a, b) < v.E;
     }
-    ++t.rechecks;
-    return sqdist64<DIM>(a, b) < v.E;
+    t.hits += nb ? 1u : 0u;
+    return nb;
 }
 
 template <int MODE, int DIM>
@@ -408,15 +416,31 @@ __device__ __forceinline__ int uf_hook(int* parent, int a, int b, int& err) {
     return a < b ? a : b;
 }
 
-__device__ __forceinline__ void flush_stats(const View& v, const Tally& t, int err, int lane) {
+// Warp totals of the counters into the control block; pass 0 = count passes
+// (core identification), 1 = clustering scans.
+__device__ __forceinline__ void flush_stats(const View& v, const Tally& t, int err, int lane, int pass) {
     const unsigned r = __reduce_add_sync(kFull, t.rechecks);
     const unsigned n = __reduce_add_sync(kFull, t.tests);
+    const unsigned h = __reduce_add_sync(kFull, t.hits);
     const int e = __reduce_or_sync(kFull, (unsigned)err);
     if (lane == 0) {
+        const int k = (threadIdx.x >> 5) & 7;
         if (r) atomicAdd(&v.ctl->band_rechecks, (unsigned long long)r);
-        if (n) atomicAdd(&v.ctl->dist_tests[(threadIdx.x >> 5) & 7], (unsigned long long)n);
+        if (n) atomicAdd(&v.ctl->ptests[pass][k], (unsigned long long)n);
+        if (h) atomicAdd(&v.ctl->phits[pass][k], (unsigned long long)h);
         if (e) atomicOr(&v.ctl->err, e);
     }
+}
+
+// Most distance tests of one query over the warp's lane groups of G lanes
+// (each lane's `tests` counts its own query only) into Ctl::qmax.
+template <int G>
+__device__ __forceinline__ void flush_query_max(const View& v, unsigned tests, int lane) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) tests += __shfl_xor_sync(kFull, tests, o);
+#pragma unroll
+    for (int o = G; o < 32; o <<= 1) tests = max(tests, __shfl_xor_sync(kFull, tests, o));
+    if (lane == 0 && tests) atomicMax(&v.ctl->qmax[(threadIdx.x >> 5) & 7], (int)tests);
 }
 
 // ------------------------------------------------------- neighbour lists
@@ -750,7 +774,8 @@ __device__ __forceinline__ void decr_g(const View& v, int j, int c, int bx, Stre
             if (lists && cnt1 < v.min_pts && v.ntrack[qs1] == 1) list_remove(v, qs1, xs);
         }
     }
-    flush_stats(v, tally, 0, lane);
+    flush_query_max<G>(v, tally.tests, lane);
+    flush_stats(v, tally, 0, lane, 0);
 }
 
 // The count passes' lane group, chosen per stream at run time (uniform per
@@ -1160,7 +1185,8 @@ __device__ __forceinline__ void incr_g(const View& v, int j, int c, int init, in
         else
             err = kErrChunk;
     }
-    flush_stats(v, tally, err, lane);
+    flush_query_max<G>(v, tally.tests, lane);
+    flush_stats(v, tally, err, lane, 0);
 }
 
 template <int MODE, int DK>
@@ -1370,7 +1396,7 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
         }
         if (hcore) hint[start + lane] = rh[lane];
     }
-    flush_stats(v, tally, err, lane);
+    flush_stats(v, tally, err, lane, 1);
 }
 
 template <int MODE, int DK>
@@ -1445,7 +1471,7 @@ __device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx, Str
             list_store(v, a, nfound, nbuf, lane);
         }
     }
-    flush_stats(v, tally, 0, lane);
+    flush_stats(v, tally, 0, lane, 1);
 }
 
 template <int MODE, int DK>
@@ -1539,7 +1565,7 @@ __device__ __forceinline__ void label_body(const View& v, int advance, int bx, C
             }
         }
     }
-    flush_stats(v, tally, 0, lane);
+    flush_stats(v, tally, 0, lane, 1);
     if (bx == 0 && threadIdx.x == 0) {
         v.ctl->union_next = 0;                // the next clustering's queue; not read here
         if (advance) v.ctl->slide += 1;       // no reader here

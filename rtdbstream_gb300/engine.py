@@ -56,7 +56,10 @@ class Stats(ctypes.Structure):
                 ("cell_side", ctypes.c_double), ("device_bytes", ctypes.c_int64),
                 ("launches_per_slide", ctypes.c_int32), ("chunks_per_slide", ctypes.c_int32),
                 ("dist_tests", ctypes.c_int64), ("reused_cores", ctypes.c_int64),
-                ("reserved", ctypes.c_int64 * 1)]
+                ("query_tests", ctypes.c_int64), ("query_hits", ctypes.c_int64),
+                ("cluster_tests", ctypes.c_int64), ("cluster_hits", ctypes.c_int64),
+                ("max_query_tests", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+                ("reserved", ctypes.c_int64 * 3)]
 
 
 PHASES = ("ingest", "sort", "decrement", "merge", "build", "increment", "union", "flatten", "label")
@@ -254,7 +257,7 @@ class Engine:
     def stats(self) -> dict:
         s = Stats()
         _check(self._lib.rtdbs_get_stats(self._h, ctypes.byref(s)))
-        return {f: getattr(s, f) for f, _ in Stats._fields_ if f != "reserved"}
+        return {f: getattr(s, f) for f, _ in Stats._fields_ if not f.startswith("reserved")}
 
 
 def make_params(dim: int, window_size: int, stride_size: int, radius: float, min_pts: int,

@@ -42,7 +42,7 @@ def test_library_is_sm103a_build():
 
 
 def test_abi_version_and_status_strings(lib):
-    assert lib.rtdbs_abi_version() == 1
+    assert lib.rtdbs_abi_version() == 2
     assert lib.rtdbs_status_string(0) == b"ok"
     assert lib.rtdbs_status_string(-5) == b"device-side bound hit"
 
