@@ -221,12 +221,15 @@ RTDBS_API int rtdbs_get_stats(rtdbs_engine* engine, rtdbs_stats* stats);
  * n slots).  Working memory is one static device array of about 3.4 MB,
  * part of the library: every GPU that loads the library holds it until the
  * process exits.  The first call on a device looks up that array's device
- * address (with that device current); make the first call before any stream
- * capture.  All calls share the array: calls whose work overlaps on a GPU
- * race and corrupt each other's results, so serialise them.  Runs on
- * cuda_stream (a cudaStream_t, NULL = default stream) and returns after the
- * stream has finished.  Returns RTDBS_ERR_INVALID for n above the limit or
- * bad arguments, RTDBS_ERR_DEVICE if a device-side bound was hit. */
+ * address, with that device current.  All calls share the array: calls whose
+ * work overlaps on a GPU race and corrupt each other's results, so serialise
+ * them.  Runs on cuda_stream (a cudaStream_t, NULL = default stream) and
+ * waits for that stream twice (for the points' bounding box, and at the end),
+ * so it must not be called while the stream is being captured into a graph.
+ * Returns RTDBS_ERR_INVALID for n above the limit or bad arguments,
+ * RTDBS_ERR_CUDA if a runtime call fails and RTDBS_ERR_DEVICE if a device-side
+ * bound was hit, with the text in rtdbs_last_error; an error return comes
+ * after the stream has finished the call's work. */
 RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int32_t n, int32_t dim, double eps,
                                            int32_t min_pts, int32_t precision, int32_t* d_label,
                                            int32_t* d_cluster_id, void* cuda_stream);

@@ -28,14 +28,19 @@ namespace {
 
 thread_local std::string g_last_error;
 
-int fail(int status, const char* fmt, ...) {
+int vfail(int status, const char* fmt, va_list ap) {
     char buf[512];
-    va_list ap;
-    va_start(ap, fmt);
     vsnprintf(buf, sizeof(buf), fmt, ap);
-    va_end(ap);
     g_last_error = buf;
     return status;
+}
+
+int fail(int status, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    const int r = vfail(status, fmt, ap);
+    va_end(ap);
+    return r;
 }
 
 #define CUDA_TRY(expr)                                                                  \
@@ -75,38 +80,25 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 }  // namespace
 
-struct rtdbs_engine {
-    rtdbs_params p{};
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    View v{};
-    int chunk = 0;           // C
-    int staging_points = 0;  // capacity of the staging buffer in points
-    void* dev_block = nullptr;
-    size_t dev_bytes = 0;
-    Ctl* h_ctl = nullptr;    // pinned mirror of the control block
-    bool geometry_ready = false;
-    bool loaded = false;
-    cudaGraphExec_t slide_graph = nullptr;
-    // side stream for the decrement pass beside the sort (made on the first slide)
-    cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    double cell_side = 0.0;
-};
+namespace rtdbs {
 
-namespace {
+int set_error(int status, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    const int r = vfail(status, fmt, ap);
+    va_end(ap);
+    return r;
+}
 
-// Grid geometry: cell side L = Eps (1 + 2^-12) / K with K cells per Eps (the
-// margin covers the rounding of both predicates and of the double cell
-// coordinate, so neighbours are at most K cells apart per axis), clamped
-// extents over the bounding box, one bit field per axis in the key, L doubled
-// until the fields fit 50 bits.
-int set_geometry(rtdbs_engine* e, const float* bmin, const float* bmax, bool widen) {
-    const int dim = e->p.dim;
+// Cell side L = Eps (1 + 2^-12) / K with K cells per Eps (the margin covers
+// the rounding of both predicates and of the double cell coordinate, so
+// neighbours are at most K cells apart per axis), clamped extents over the
+// bounding box, one bit field per axis in the key, L doubled until the
+// fields fit 50 bits.
+int set_geometry(View& v, int dim, double eps, int cells_per_eps, const float* bmin, const float* bmax,
+                 bool widen, double* cell_side) {
     double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-    const int K = e->p.cell_mult > 0 ? e->p.cell_mult : 1;
-    double L = e->p.eps * (1.0 + 1.0 / 4096.0) / K;  // K cells per Eps: neighbours within K cells
+    double L = eps * (1.0 + 1.0 / 4096.0) / cells_per_eps;
     for (int a = 0; a < dim; ++a) {
         lo[a] = bmin[a];
         hi[a] = bmax[a];
@@ -129,10 +121,9 @@ int set_geometry(rtdbs_engine* e, const float* bmin, const float* bmax, bool wid
             while (bits[a] < 62 && (1ll << bits[a]) < ext[a]) ++bits[a];
             total += bits[a];
         }
-        if (total <= rtdbs::kKeyBitsMax) break;
+        if (total <= kKeyBitsMax) break;
         L *= 2.0;
     }
-    View& v = e->v;
     for (int a = 0; a < 3; ++a) {
         v.origin[a] = lo[a];
         v.ext[a] = ext[a];
@@ -144,8 +135,7 @@ int set_geometry(rtdbs_engine* e, const float* bmin, const float* bmax, bool wid
     v.inv_cell = 1.0 / L;
     v.key_bits = kbits;
     v.sort_passes = (kbits + 7) / 8;
-    e->cell_side = L;
-    e->geometry_ready = true;
+    if (cell_side) *cell_side = L;
     return RTDBS_OK;
 }
 
@@ -167,6 +157,39 @@ void set_band(View& v, double eps) {
     v.filter_ok = (E >= std::ldexp(1.0, -100) && E <= std::ldexp(1.0, 100)) ? 1 : 0;
     const float r = (float)eps;
     v.r2f = r * r;
+}
+
+}  // namespace rtdbs
+
+struct rtdbs_engine {
+    rtdbs_params p{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    View v{};
+    int chunk = 0;           // C
+    int staging_points = 0;  // capacity of the staging buffer in points
+    void* dev_block = nullptr;
+    size_t dev_bytes = 0;
+    Ctl* h_ctl = nullptr;    // pinned mirror of the control block
+    bool geometry_ready = false;
+    bool loaded = false;
+    cudaGraphExec_t slide_graph = nullptr;
+    // side stream for the decrement pass beside the sort (made on the first slide)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    double cell_side = 0.0;
+};
+
+namespace {
+
+// The engine's geometry: the box given in its parameters, or that of its
+// first window (widened).
+int engine_geometry(rtdbs_engine* e, const float* bmin, const float* bmax, bool widen) {
+    const int K = e->p.cell_mult > 0 ? e->p.cell_mult : 1;
+    const int rc = rtdbs::set_geometry(e->v, e->p.dim, e->p.eps, K, bmin, bmax, widen, &e->cell_side);
+    if (rc == RTDBS_OK) e->geometry_ready = true;
+    return rc;
 }
 
 struct Part {
@@ -412,11 +435,11 @@ int rtdbs_create(const rtdbs_params* params, void* cuda_stream, rtdbs_engine** o
     v.min_pts = p.min_pts;
     v.units = p.window / p.stride;
     v.precision = p.precision;
-    set_band(v, p.eps);
+    rtdbs::set_band(v, p.eps);
     int rc = allocate(e);
     if (rc == RTDBS_OK) {
         v.chunk = e->chunk;
-        if (p.has_bbox) rc = set_geometry(e, p.bbox_min, p.bbox_max, false);
+        if (p.has_bbox) rc = engine_geometry(e, p.bbox_min, p.bbox_max, false);
     }
     if (rc != RTDBS_OK) {
         rtdbs_destroy(e);
@@ -468,7 +491,7 @@ int rtdbs_load_window(rtdbs_engine* e, const float* points, int points_on_device
             mn[a] = lo;
             mx[a] = hi;
         }
-        int rc = set_geometry(e, mn, mx, true);
+        int rc = engine_geometry(e, mn, mx, true);
         if (rc != RTDBS_OK) return rc;
     }
     // Restart from an empty window.
@@ -722,6 +745,7 @@ namespace {
 
 void pool_drop_shape(rtdbs_pool* p) {
     if (p->graph) {
+        cudaStreamSynchronize(p->stream);  // a replay of it may still be queued
         cudaGraphExecDestroy(p->graph);
         p->graph = nullptr;
     }
@@ -817,13 +841,16 @@ int pool_build_shape(rtdbs_pool* p, const std::vector<int>& ids) {
     for (auto& it : all_items) it.c = 0;  // cluster phases size by W only
     for (int ph = rtdbs::kBatchDamage; ph <= rtdbs::kBatchLabel; ++ph) add_launches(ph, all_items);
     if (img.size() > p->tables_cap) {
+        // (cudaFree waits for the rounds that still read the old buffer)
         if (p->d_tables) cudaFree(p->d_tables);
         p->d_tables = nullptr;
         CUDA_TRY(cudaMalloc((void**)&p->d_tables, img.size()));
         p->tables_cap = img.size();
     }
-    CUDA_TRY(cudaStreamSynchronize(p->stream));  // the tables may be in use by the last round
-    CUDA_TRY(cudaMemcpy(p->d_tables, img.data(), img.size(), cudaMemcpyHostToDevice));
+    // Stream-ordered: the copy lands after the rounds already queued (which
+    // read the previous tables) and before this round; from pageable memory
+    // the call returns once the image is staged, so the host never waits.
+    CUDA_TRY(cudaMemcpyAsync(p->d_tables, img.data(), img.size(), cudaMemcpyHostToDevice, p->stream));
     p->plan = std::move(plan);
     p->input_off = std::move(off);
     p->input_floats = floats;

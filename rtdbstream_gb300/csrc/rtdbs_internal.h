@@ -171,6 +171,22 @@ cudaError_t launch_cluster(const View& v, int precision, int advance, cudaStream
 cudaError_t launch_counts_by_slot(const View& v, int* nn_by_slot, cudaStream_t s);
 cudaError_t configure_kernels();
 
+// Host helpers shared by the engine and the allocation-free entry point
+// (rtdbs_engine.cpp).
+// Records the text rtdbs_last_error returns on this thread; returns status.
+int set_error(int status, const char* fmt, ...);
+// FP32 filter band of the FP64 predicate and the FP32 radius (View::lo, hi,
+// E, filter_ok, r2f) for this Eps.
+void set_band(View& v, double eps);
+// Grid geometry of View v (origin, extents, key fields, inv_cell, key_bits,
+// sort_passes) for cells of side Eps (1 + 2^-12) / cells_per_eps over the
+// box [bmin, bmax] of `dim` axes, widened by 25% (and at least 4 cells) when
+// `widen`; the cell side doubles until the key fits kKeyBitsMax bits.
+// Returns RTDBS_OK or RTDBS_ERR_INVALID (empty or non-finite box); the side
+// used goes to *cell_side.
+int set_geometry(View& v, int dim, double eps, int cells_per_eps, const float* bmin, const float* bmax,
+                 bool widen, double* cell_side);
+
 // ------------------------------------------------------------ batched launches
 // One launch of a phase covers many streams: block b belongs to the item i
 // with prefix[i] <= b < prefix[i+1] and runs that stream's kernel body with

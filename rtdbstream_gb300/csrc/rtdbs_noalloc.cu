@@ -109,12 +109,15 @@ __global__ void k_noalloc_bbox(const float* pts, int n, int dim, float* box) {
 int scratch_for_current_device(unsigned char** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
-        return RTDBS_ERR_NO_DEVICE;
+        return rtdbs::set_error(RTDBS_ERR_NO_DEVICE, "noalloc: no current CUDA device (or ordinal >= %d)",
+                                kMaxDevices);
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     if (!g_scratch_ptr[dev]) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-        if (e != cudaSuccess || !p) return RTDBS_ERR_CUDA;
+        if (e != cudaSuccess || !p)
+            return rtdbs::set_error(RTDBS_ERR_CUDA, "noalloc: cudaGetSymbolAddress of the scratch array failed: %s",
+                                    cudaGetErrorString(e));
         g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
     }
     *out = g_scratch_ptr[dev];
@@ -127,30 +130,44 @@ extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int
                                                       double eps, int32_t min_pts, int32_t precision,
                                                       int32_t* d_label, int32_t* d_cluster_id,
                                                       void* cuda_stream) {
-    if (!d_points || !d_label || !d_cluster_id) return RTDBS_ERR_INVALID;
-    if (n < 0 || n > kMaxPoints) return RTDBS_ERR_INVALID;  // beyond the scratch array
-    if (dim < 1 || dim > 3) return RTDBS_ERR_INVALID;
-    if (!(eps > 0.0) || !std::isfinite(eps)) return RTDBS_ERR_INVALID;
-    if (precision != RTDBS_PREC_FP64 && precision != RTDBS_PREC_FP32) return RTDBS_ERR_INVALID;
+    using rtdbs::set_error;
+    if (!d_points || !d_label || !d_cluster_id)
+        return set_error(RTDBS_ERR_INVALID, "noalloc: points, label and cluster_id must not be NULL");
+    if (n < 0 || n > kMaxPoints)  // beyond the scratch array
+        return set_error(RTDBS_ERR_INVALID, "noalloc: n = %d outside 0..%d (RTDBS_NOALLOC_MAX_POINTS)", n,
+                         kMaxPoints);
+    if (dim < 1 || dim > 3) return set_error(RTDBS_ERR_INVALID, "noalloc: dim must be 1..3 (got %d)", dim);
+    if (!(eps > 0.0) || !std::isfinite(eps))
+        return set_error(RTDBS_ERR_INVALID, "noalloc: eps must be finite and > 0");
+    if (precision != RTDBS_PREC_FP64 && precision != RTDBS_PREC_FP32)
+        return set_error(RTDBS_ERR_INVALID, "noalloc: unknown precision mode %d", precision);
     if (n == 0) return RTDBS_OK;
     unsigned char* base = nullptr;
     int rc = scratch_for_current_device(&base);
     if (rc != RTDBS_OK) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
 
-#define NOALLOC_TRY(expr)                                                      \
-    do {                                                                       \
-        const cudaError_t _e = (expr);                                         \
-        if (_e != cudaSuccess) return RTDBS_ERR_CUDA;                          \
+    // Once work is queued on s, an error return first waits for it, so that
+    // an error also means the scratch array is no longer in use.
+    bool queued = false;
+#define NOALLOC_TRY(expr)                                                                              \
+    do {                                                                                               \
+        const cudaError_t _e = (expr);                                                                 \
+        if (_e != cudaSuccess) {                                                                       \
+            if (queued) cudaStreamSynchronize(s);                                                      \
+            return set_error(RTDBS_ERR_CUDA, "noalloc: %s failed: %s", #expr, cudaGetErrorString(_e)); \
+        }                                                                                              \
     } while (0)
 
     // Every call reuses the array, which still holds the previous call's
     // data: the cell tables (generation tags) and the control block must
     // start at zero; everything else is rewritten before it is read.
+    queued = true;
     NOALLOC_TRY(cudaMemsetAsync(base + kOffTable0, 0, sizeof(ulonglong2) * kTableSlots * 2, s));
     NOALLOC_TRY(cudaMemsetAsync(base + kOffCtl, 0, sizeof(Ctl), s));
 
-    // Bounding box -> grid geometry (same rules as an engine without a box).
+    // Bounding box -> grid geometry (same rules as an engine without a box):
+    // the box comes back to the host, the one wait inside the call.
     float* d_box = reinterpret_cast<float*>(base + kOffBox);
     k_noalloc_bbox<<<1, 1024, 0, s>>>(d_points, n, dim, d_box);
     NOALLOC_TRY(cudaGetLastError());
@@ -170,47 +187,9 @@ extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int
     v.min_pts = min_pts;
     v.chunk = n;
     v.precision = precision;
-    const double E = eps * eps, m = 1.0 / 1048576.0;
-    float flo = (float)(E * (1.0 - m)), fhi = (float)(E * (1.0 + m));
-    if ((double)flo > E * (1.0 - m)) flo = std::nextafter(flo, 0.0f);
-    if ((double)fhi < E * (1.0 + m)) fhi = std::nextafter(fhi, INFINITY);
-    v.lo = flo;
-    v.hi = fhi;
-    v.E = E;
-    v.filter_ok = (E >= std::ldexp(1.0, -100) && E <= std::ldexp(1.0, 100)) ? 1 : 0;
-    const float r = (float)eps;
-    v.r2f = r * r;
-    double L = eps * (1.0 + 1.0 / 4096.0);
-    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-    for (int a = 0; a < dim; ++a) {
-        const double mg = std::max(0.25 * ((double)box[3 + a] - box[a]), 4.0 * L);
-        lo[a] = box[a] - mg;
-        hi[a] = box[3 + a] + mg;
-    }
-    long long ext[3] = {1, 1, 1};
-    int bits[3] = {0, 0, 0};
-    for (int guard = 0; guard < 4096; ++guard) {
-        int total = 0;
-        for (int a = 0; a < dim; ++a) {
-            const double cells = std::floor((hi[a] - lo[a]) / L) + 1.0;
-            ext[a] = cells < 4.0e15 ? (long long)cells : (long long)4.0e15;
-            bits[a] = 0;
-            while (bits[a] < 62 && (1ll << bits[a]) < ext[a]) ++bits[a];
-            total += bits[a];
-        }
-        if (total <= rtdbs::kKeyBitsMax) break;
-        L *= 2.0;
-    }
-    for (int a = 0; a < 3; ++a) {
-        v.origin[a] = lo[a];
-        v.ext[a] = ext[a];
-    }
-    v.shift[2] = 0;
-    v.shift[1] = bits[2];
-    v.shift[0] = bits[1] + bits[2];
-    v.inv_cell = 1.0 / L;
-    v.key_bits = bits[0] + bits[1] + bits[2];
-    v.sort_passes = (v.key_bits + 7) / 8;
+    rtdbs::set_band(v, eps);
+    rc = rtdbs::set_geometry(v, dim, eps, 1, box, box + 3, true, nullptr);
+    if (rc != RTDBS_OK) return rc;  // nothing is queued after the wait above
     v.pbits = 15;
     v.pmask = (unsigned)(kTableSlots - 1);
     v.max_items = kMaxItems;
@@ -247,5 +226,8 @@ extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int
     NOALLOC_TRY(cudaMemcpyAsync(&err, &v.ctl->err, sizeof(int), cudaMemcpyDeviceToHost, s));
     NOALLOC_TRY(cudaStreamSynchronize(s));
 #undef NOALLOC_TRY
-    return err ? RTDBS_ERR_DEVICE : RTDBS_OK;
+    if (err)
+        return set_error(RTDBS_ERR_DEVICE, "noalloc: device error bits 0x%x (1 table full, 2 union-find bound, "
+                         "4 work list full, 8 chunk bookkeeping)", err);
+    return RTDBS_OK;
 }

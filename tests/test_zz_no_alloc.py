@@ -4,14 +4,21 @@ the GPU's memory in its own pool, or a latency path that cannot take
 cudaMalloc's implicit synchronisation).
 
 Called through the C ABI and compared bit-exactly with the allocating entry
-points (rtdbs_load_window + rtdbs_cluster + rtdbs_get_counts-free output) on
-two calls in a row.  This file is collected last on purpose.
+points (rtdbs_load_window + rtdbs_cluster) and with the CPU oracle on two
+calls in a row, with another window clustered in between.  Also checks that a
+warm call leaves the device's free memory unchanged, and that a call works as
+the first kernel launch of a fresh process.  This file is collected last on
+purpose.
 """
 import ctypes
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
 
+import oracle as O
 from rtdbstream_gb300 import Engine
 from rtdbstream_gb300 import engine as E
 from rtdbstream_gb300 import workloads as wl
@@ -19,6 +26,7 @@ from rtdbstream_gb300 import workloads as wl
 pytestmark = pytest.mark.gpu
 
 MAX_POINTS = 16384
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 @pytest.fixture(scope="module")
@@ -26,6 +34,7 @@ def noalloc():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no GPU")
+    O.build(ref=False)
     L = E.load_library()
     fn = L.rtdbs_cluster_window_noalloc
     fn.restype = ctypes.c_int
@@ -34,17 +43,24 @@ def noalloc():
     return fn
 
 
-def call_noalloc(fn, pts, eps, mp, precision):
+def device_buffers(pts):
     import torch
 
     d = torch.from_numpy(np.ascontiguousarray(pts, np.float32)).cuda()
     n = len(pts)
     lab = torch.full((n,), -7, dtype=torch.int32, device="cuda")
     cid = torch.full((n,), -7, dtype=torch.int32, device="cuda")
+    return d, lab, cid
+
+
+def call_noalloc(fn, pts, eps, mp, precision, bufs=None):
+    import torch
+
+    d, lab, cid = bufs or device_buffers(pts)
     stream = torch.cuda.current_stream().cuda_stream
-    rc = fn(d.data_ptr(), n, pts.shape[1], float(eps), int(mp),
+    rc = fn(d.data_ptr(), len(pts), pts.shape[1], float(eps), int(mp),
             E.PREC_FP64 if precision == "fp64" else E.PREC_FP32, lab.data_ptr(), cid.data_ptr(), stream)
-    assert rc == 0, f"rtdbs_cluster_window_noalloc returned {rc}"
+    assert rc == 0, f"rtdbs_cluster_window_noalloc returned {rc}: {E.load_library().rtdbs_last_error()}"
     return lab.cpu().numpy(), cid.cpu().numpy()
 
 
@@ -59,21 +75,74 @@ CASES = [
     ("mix2d", lambda: wl.gaussian_mixture(6_000, dim=2, k=8, box=25.0, seed=41), 0.5, 5, "fp64"),
     ("walk3d_max", lambda: wl.random_walkers(MAX_POINTS, n_walkers=40, seed=42), 3.3e-3, 10, "fp64"),
     ("band3d_fp32", lambda: wl.offset_band_points(5_000, 1e-3, partner_frac=0.3, seed=43), 1e-3, 2, "fp32"),
+    ("stk1d", lambda: wl.gaussian_mixture(4_000, dim=1, k=6, box=10.0, sigma=0.3, seed=44), 0.01, 4, "fp64"),
+    ("mix3d_mp40", lambda: wl.gaussian_mixture(8_000, dim=3, k=6, box=12.0, seed=45), 0.9, 40, "fp64"),
 ]
 
 
 @pytest.mark.parametrize("name,gen,eps,mp,precision", CASES, ids=[c[0] for c in CASES])
-def test_noalloc_matches_allocating_entry_points_twice(noalloc, name, gen, eps, mp, precision):
+def test_noalloc_matches_engine_and_oracle_twice(noalloc, name, gen, eps, mp, precision):
     pts = gen()
     exp_lab, exp_cid = call_engine(pts, eps, mp, precision)
-    # an unrelated call first, so the second call of this case starts from a
-    # scratch array that holds another window's data
+    mode = O.MODE_FP64 if precision == "fp64" else O.MODE_FP32
+    _, o_lab, o_cid, _ = O.window_grid(pts, eps, mp, mode)
+    assert np.array_equal(exp_lab, o_lab) and np.array_equal(exp_cid, o_cid), f"{name}: engine vs oracle"
+    # an unrelated call between the two, so the second call of this case
+    # starts from a scratch array that holds another window's data
     other = wl.gaussian_mixture(3_000, dim=3, k=5, box=10.0, seed=99)
     for k in range(2):
         lab, cid = call_noalloc(noalloc, pts, eps, mp, precision)
-        assert np.array_equal(lab, exp_lab), f"{name}: labels differ on call {k + 1}"
-        assert np.array_equal(cid, exp_cid), f"{name}: ids differ on call {k + 1}"
+        assert np.array_equal(lab, o_lab), f"{name}: labels differ from the oracle on call {k + 1}"
+        assert np.array_equal(cid, o_cid), f"{name}: ids differ from the oracle on call {k + 1}"
+        assert np.array_equal(lab, exp_lab) and np.array_equal(cid, exp_cid), f"{name}: engine, call {k + 1}"
         call_noalloc(noalloc, other, 0.7, 4, "fp64")
+
+
+def test_noalloc_allocates_no_device_memory(noalloc):
+    import torch
+
+    pts = wl.gaussian_mixture(MAX_POINTS, dim=3, k=10, box=20.0, seed=46)
+    bufs = device_buffers(pts)
+    call_noalloc(noalloc, pts, 0.8, 6, "fp64", bufs)  # warm: set-up done
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        call_noalloc(noalloc, pts, 0.8, 6, "fp64", bufs)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, f"device free memory changed by {free0 - free1} bytes"
+
+
+def test_noalloc_first_kernel_launch_of_a_fresh_process(noalloc):
+    """The set-up on the first call (the device address of the static
+    array) works when the library has launched nothing else in the process."""
+    code = r'''
+import ctypes, sys
+import numpy as np
+sys.path.insert(0, ROOT_DIR)
+from rtdbstream_gb300 import engine as E
+from rtdbstream_gb300 import workloads as wl
+import oracle as O
+import torch  # device buffers only: the call below is the library's first launch
+L = E.load_library()
+fn = L.rtdbs_cluster_window_noalloc
+fn.restype = ctypes.c_int
+fn.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_int32,
+               ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+pts = wl.gaussian_mixture(5_000, dim=2, k=6, box=25.0, seed=47)
+n = len(pts)
+d = torch.from_numpy(pts).cuda()
+lab = torch.empty(n, dtype=torch.int32, device="cuda")
+cid = torch.empty(n, dtype=torch.int32, device="cuda")
+rc = fn(d.data_ptr(), n, 2, 0.5, 5, E.PREC_FP64, lab.data_ptr(), cid.data_ptr(), None)
+assert rc == 0, (rc, L.rtdbs_last_error())
+_, elab, ecid, _ = O.window_grid(pts, 0.5, 5, O.MODE_FP64)
+assert np.array_equal(lab.cpu().numpy(), elab) and np.array_equal(cid.cpu().numpy(), ecid)
+print("fresh-process call ok")
+'''.replace("ROOT_DIR", repr(ROOT))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "fresh-process call ok" in r.stdout
 
 
 def test_noalloc_rejects_oversized_window(noalloc):
@@ -84,3 +153,4 @@ def test_noalloc_rejects_oversized_window(noalloc):
     out = torch.empty(n, dtype=torch.int32, device="cuda")
     rc = noalloc(d.data_ptr(), n, 2, 0.5, 4, E.PREC_FP64, out.data_ptr(), out.data_ptr(), None)
     assert rc == E.RTDBS_ERR_INVALID
+    assert b"RTDBS_NOALLOC_MAX_POINTS" in E.load_library().rtdbs_last_error()
