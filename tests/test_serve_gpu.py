@@ -87,3 +87,71 @@ def test_server_admits_as_memory_frees(torch_stream):
     assert not srv.waiting and all(st.sid is None for _, _, st in streams)
     assert srv.pool.stats()["streams"] == 0
     srv.close()
+
+
+def test_budget_bound_results_match_streams_alone(torch_stream):
+    """The mix is bigger than the budget: streams wait, are admitted as
+    others finish, and every stream's final window is still exact."""
+    streams = make_streams(20, seed=13)
+    costs = [stream_bytes(make_params(sp.dim, sp.window, sp.stride, sp.eps, sp.min_pts)) for sp, _, _ in streams]
+    budget = sum(sorted(costs)[-5:]) + 1        # any 5 streams fit, not all 20
+    srv = SlideServer(hbm_budget_bytes=budget, stream=torch_stream.cuda_stream, depth=3)
+    t, tgt = poisson_arrivals(rate=600.0, duration=0.4, n_streams=len(streams), seed=7)
+    # every stream also gets 2..4 requests appended after the Poisson ones
+    rng = np.random.default_rng(8)
+    extra = np.repeat(np.arange(len(streams)), rng.integers(2, 5, len(streams)))
+    t2 = np.concatenate([t, t.max() + 0.001 * np.arange(1, len(extra) + 1)])
+    tgt2 = np.concatenate([tgt, extra.astype(tgt.dtype)])
+    per = np.bincount(tgt2, minlength=len(streams))
+    for (sp, pts, st), n_req in zip(streams, per):
+        st.requests_total = int(n_req)
+        srv.add(st)
+    assert len(srv.waiting) > 0
+    # every stream's final result, read just before it leaves the pool
+    finals = {}
+    orig_retire = srv._retire
+
+    def retire_and_keep(i):
+        finals[i] = srv.pool.outputs(srv.streams[i].sid)
+        orig_retire(i)
+
+    srv._retire = retire_and_keep
+    res = srv.run(t2, tgt2)
+    assert res["requests"] == len(t2)
+    assert res["admission_wait_ms_p50"] is not None
+    assert not srv.waiting and srv.pool.stats()["streams"] == 0
+    for i, (sp, pts, st) in enumerate(streams):
+        assert st.done == per[i]
+        win = replay(sp, pts, st.done)
+        _, elab, ecid, _ = O.window_grid(win, sp.eps, sp.min_pts, O.MODE_FP64)
+        lab, cid = finals[i]
+        assert np.array_equal(lab, elab) and np.array_equal(cid, ecid), f"stream {i}"
+    srv.close()
+
+
+def test_budget_refusals(torch_stream):
+    """A stream larger than the whole budget is refused when added; requests
+    that only waiting streams could serve, with nothing left to free memory,
+    end the run with RTDBS_ERR_BUDGET instead of waiting forever."""
+    from rtdbstream_gb300 import RtdbsError
+    from rtdbstream_gb300.engine import RTDBS_ERR_BUDGET
+
+    streams = make_streams(3, seed=14)
+    costs = [stream_bytes(make_params(sp.dim, sp.window, sp.stride, sp.eps, sp.min_pts)) for sp, _, _ in streams]
+    srv = SlideServer(hbm_budget_bytes=min(costs) - 1, stream=torch_stream.cuda_stream)
+    with pytest.raises(RtdbsError) as e:
+        srv.add(streams[int(np.argmin(costs))][2])
+    assert e.value.status == RTDBS_ERR_BUDGET
+    srv.close()
+    # budget for one stream: the first is admitted (no request limit and no
+    # requests), the second waits and has requests
+    order = np.argsort(costs)[::-1]
+    a, b = streams[order[0]][2], streams[order[1]][2]
+    srv = SlideServer(hbm_budget_bytes=costs[order[0]] + 1, stream=torch_stream.cuda_stream)
+    srv.add(a)
+    srv.add(b)
+    assert a.sid is not None and b.sid is None
+    with pytest.raises(RtdbsError) as e:
+        srv.run(np.array([0.0, 0.001]), np.array([1, 1]))
+    assert e.value.status == RTDBS_ERR_BUDGET
+    srv.close()
