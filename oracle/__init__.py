@@ -24,7 +24,17 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libref_cpu.so")
-REFERENCE_TREE = os.environ.get("RTDBS_REFERENCE_TREE", "/root/reference")
+
+def reference_tree() -> Optional[str]:
+    """Where the reference's sources lie: $RTDBS_REFERENCE_TREE, else the
+    location the build recipe (oracle/Makefile) reads them from; None where
+    they are absent (the GPU machine has only this package's restatement)."""
+    tree = os.environ.get("RTDBS_REFERENCE_TREE")
+    if not tree:
+        r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+        tree = r.stdout.strip()
+    return tree if tree and os.path.isdir(os.path.join(tree, "src", "dbscan")) else None
+
 
 MODE_FP64 = 0
 MODE_FP32 = 1
@@ -37,10 +47,15 @@ class OracleStats(ctypes.Structure):
 
 def build(ref: bool = True) -> None:
     """Compile liboracle.so (always) and the reference CPU library (when the
-    reference tree exists on this machine)."""
+    reference's sources are present on this machine; otherwise says so)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    if ref and os.path.isdir(os.path.join(REFERENCE_TREE, "src", "dbscan")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REFERENCE_TREE}"], check=True)
+    if not ref:
+        return
+    tree = reference_tree()
+    if tree:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={tree}"], check=True)
+    else:
+        print("oracle: reference sources not present here; only the restatement is built")
 
 
 _lib = None

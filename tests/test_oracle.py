@@ -92,8 +92,8 @@ def test_band_bounds():
     assert not ok_tiny
 
 
-@pytest.mark.skipif(O.ref_lib() is None and not os.path.isdir(O.REFERENCE_TREE),
-                    reason="reference tree not present")
+@pytest.mark.skipif(O.ref_lib() is None and O.reference_tree() is None,
+                    reason="reference sources not present (only the committed fixtures pin the oracle here)")
 @pytest.mark.parametrize("dim,seed", [(1, 31), (2, 32), (3, 33)])
 def test_live_reference_vs_restatement(oracle_lib, dim, seed):
     pts = wl.gaussian_mixture(1500, dim=dim, k=6, box=12.0, seed=seed)
