@@ -831,16 +831,20 @@ def run_serving(args, dev, stream, world=1, rank=0, n_streams=1000, loads=(0.3, 
     cap = srv.run(t_all, tgt_all)
     cap_rps = cap["requests"] / cap["wall_s"]
     cap_value, _ = combined(cap)
-    sweep = []
-    for f in loads:
-        rate = f * cap_rps
-        t, tgt = poisson_arrivals(rate, duration, n_mine, seed=int(f * 100) + 1000 * rank)
-        r = srv.run(t, tgt)
-        v, p99max = combined(r)
-        sweep.append({"offered_requests_per_s": rate * world, "offered_fraction": f, "requests": r["requests"],
-                      "slid_points_per_s": v, "latency_ms_p50": r["latency_ms_p50"],
-                      "latency_ms_p99": r["latency_ms_p99"], "latency_ms_p99_max_over_ranks": p99max,
-                      "mean_round_size": r["mean_round_size"]})
+    sweeps = {}
+    for depth in (1, 2):  # rounds formed as the previous completes / one queued behind it
+        srv.depth = depth
+        sweep = []
+        for f in loads:
+            rate = f * cap_rps
+            t, tgt = poisson_arrivals(rate, duration, n_mine, seed=int(f * 100) + 1000 * rank)
+            r = srv.run(t, tgt)
+            v, p99max = combined(r)
+            sweep.append({"offered_requests_per_s": rate * world, "offered_fraction": f, "requests": r["requests"],
+                          "slid_points_per_s": v, "latency_ms_p50": r["latency_ms_p50"],
+                          "latency_ms_p99": r["latency_ms_p99"], "latency_ms_p99_max_over_ranks": p99max,
+                          "mean_round_size": r["mean_round_size"]})
+        sweeps[depth] = sweep
     st = srv.pool.stats()
     srv.close()
 
@@ -866,10 +870,11 @@ def run_serving(args, dev, stream, world=1, rank=0, n_streams=1000, loads=(0.3, 
     done_all = all(s.done == 3 for s in streams)
     srv.close()
     return {"workload": f"{n_streams} streams (the batched mix, W 1k..200k), Poisson slide requests, "
-                        f"HBM budget 120 GB ({st['bytes_in_use'] / 1e9:.1f} GB admitted on rank 0), rounds pipelined "
-                        f"(the next round is queued while one runs)",
+                        f"HBM budget 120 GB ({st['bytes_in_use'] / 1e9:.1f} GB admitted on rank 0); sweep: a round is formed "
+                        f"when the previous completes; sweep_pipelined: one more round queued while one runs",
             "capacity_requests_per_s": cap_rps * world, "capacity_slid_points_per_s": cap_value,
-            "sweep": sweep,
+            "sweep": sweeps[1],
+            "sweep_pipelined": sweeps[2],
             "budget_bound": {"budget_bytes": budget, "mix_bytes": int(sum(costs)),
                              "streams_waiting_at_start": waiting0, "requests": rb["requests"],
                              "all_streams_served_and_retired": done_all,

@@ -704,12 +704,14 @@ __global__ void __launch_bounds__(kSortRun) k_runmerge(View v, int j, int c, int
 // per warp, so two queries' dependent loads overlap) or 32; the 25 rows of the
 // two-cells-per-Eps stencil need the whole warp.
 
+constexpr int kFlattenQueue = 128;  // list rebuilds a flatten block queues for its warps to share
+
 struct StreamSmem {
     int rstart[8][kMaxRows], rpre[8][kMaxRows + 1];
     int grstart[8][2][kMaxRows], grpre[8][2][kMaxRows + 1];  // per lane group (count passes)
     int nbuf[8][kListCap];
     int gnbuf[8][2][kListCap];
-    int queue[256];  // k_flatten: positions whose lists are rebuilt, in the block's tile
+    int queue[kFlattenQueue];  // k_flatten: positions of the block whose lists are rebuilt
     int nq;
 };
 
@@ -1294,10 +1296,11 @@ struct ClusterSmem {
     int home_root[kClusterThreads / 32][32];
     float4 home_pt[kClusterThreads / 32][32];
     int rstart[kClusterThreads / 32][kMaxRows], rpre[kClusterThreads / 32][kMaxRows + 1];
+    int seg_next;  // k_union: next item of the block's own segment
 };
 
 template <int MODE, int DK>
-__device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
+__device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm, int bx, int nbx) {
     constexpr int DIM = DK & 3, K = (DK >> 2) + 1;  // dimension, cells per Eps
     float4(&home_pt)[kClusterThreads / 32][32] = sm.home_pt;
     int(&rstart)[kClusterThreads / 32][kMaxRows] = sm.rstart;
@@ -1320,17 +1323,35 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
     volatile int* hint = v.sroot;
     Tally tally;
     int err = 0;
-    // Warps take batches of v.grab consecutive work items (neighbouring
-    // cells: candidate loads reuse L1) from a counter, so uneven items do not
-    // leave warps idle at the end.
+    // Work split: the first 4/5 of the items in one contiguous segment per
+    // block, handed out an item at a time from a shared-memory counter (the
+    // block's warps take neighbouring cells, so candidate loads reuse L1);
+    // the rest from the stream's queue, v.grab consecutive items at a time,
+    // so blocks whose segment was cheap take more of it and uneven items do
+    // not leave warps idle at the end.
+    const int nstat = nitems - nitems / 5;
+    const int seg = (nstat + nbx - 1) / nbx;
+    const int s0 = min(bx * seg, nstat), s1 = min(s0 + seg, nstat);
+    if (threadIdx.x == 0) sm.seg_next = s0;
+    __syncthreads();
+    bool own = true;  // the block's segment may still hold items
     int it1 = 0;
     for (int itx = nitems;;) {
         if (itx >= it1) {
-            int got = 0;
-            if (lane == 0) got = atomicAdd(&v.ctl->union_next, v.grab);
-            itx = __shfl_sync(kFull, got, 0);
-            if (itx >= nitems) break;
-            it1 = min(itx + v.grab, nitems);
+            int got = 0, from_seg = 0;
+            if (lane == 0) {
+                if (own) {
+                    got = atomicAdd(&sm.seg_next, 1);
+                    from_seg = got < s1 ? 1 : 0;
+                }
+                if (!from_seg) got = nstat + atomicAdd(&v.ctl->union_next, v.grab);
+            }
+            got = __shfl_sync(kFull, got, 0);
+            from_seg = __shfl_sync(kFull, from_seg, 0);
+            own = from_seg != 0;
+            if (got >= nitems) break;
+            itx = got;
+            it1 = from_seg ? got + 1 : min(got + v.grab, nitems);
         }
         const int2 item = v.items[itx++];
         const int start = item.x, len = item.y;
@@ -1402,16 +1423,41 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
 template <int MODE, int DK>
 __global__ void __launch_bounds__(kClusterThreads, 8) k_union(View v) {
     __shared__ ClusterSmem sm;
-    union_body<MODE, DK>(v, sm);
+    union_body<MODE, DK>(v, sm, blockIdx.x, gridDim.x);
+}
+
+// The neighbour list of the non-core point at sorted position `at`, from one
+// scan of the current grid (called by the whole warp).
+template <int MODE, int DIM, int K>
+__device__ __forceinline__ void rebuild_list(const View& v, int at, int cur, unsigned gen, int lane, int* rstart,
+                                             int* rpre, int* nbuf, Tally& tally) {
+    const float4* spt = v.spt[cur];
+    const float4 ap = spt[at];
+    const int a = slot_of(ap);
+    int rs, re;
+    row_ranges<DIM, false, K>(v, v.table[cur], gen, v.skey[cur][at], lane, rs, re);
+    const int total = candidate_stream<Stencil<DIM, false, K>::kRows>(rs, re, 0, lane, rstart, rpre);
+    int r = 0, nfound = 0;
+    for (int base = 0; base < total; base += 32) {
+        const int idx = base + lane;
+        bool nb = false;
+        int qs = -1;
+        if (idx < total) {
+            const float4 q = spt[stream_pos(idx, r, rstart, rpre)];
+            qs = slot_of(q);
+            nb = qs != a && is_nbr<MODE, DIM>(v, ap, q, tally);
+        }
+        nfound = list_collect(nb, qs, nfound, v.list_cap, nbuf, lane);
+    }
+    list_store(v, a, nfound, nbuf, lane);
 }
 
 // Root of every core point, walked from the position's root hint.  Without
 // neighbour lists: by sorted position (-1 for non-core points), for the grid
 // scan of k_label.  With lists: by slot (rslot), which k_border turns into
 // the outputs; and a point below MinPts without a list (it lost core status
-// this slide) gets its list rebuilt here from one scan of the final grid --
-// each block queues such points of its 256-position tile in shared memory
-// and rebuilds them warp by warp.
+// this slide) gets its list rebuilt here from one scan of the final grid, by
+// the warp whose 32 positions hold it.
 template <int MODE, int DK>
 __device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx, StreamSmem& sm) {
     constexpr int DIM = DK & 3, K = (DK >> 2) + 1;  // dimension, cells per Eps
@@ -1429,53 +1475,50 @@ __device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx, Str
     int(&rpre)[8][kMaxRows + 1] = sm.rpre;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
     const unsigned gen = gen_of_build(b);
-    const float4* spt = v.spt[cur];
-    const int* sw = reinterpret_cast<const int*>(spt) + 3;  // .w = slot
+    const int* sw = reinterpret_cast<const int*>(v.spt[cur]) + 3;  // .w = slot
     int* nbuf = sm.nbuf[wib];
     Tally tally;
-    for (int p0 = bx * blockDim.x; p0 < n; p0 += nbx * blockDim.x) {
-        __syncthreads();
-        if (threadIdx.x == 0) sm.nq = 0;
-        __syncthreads();
-        const int i = p0 + threadIdx.x;
+    // Roots first (no barrier); the positions whose lists are rebuilt go to
+    // the block's queue, which its warps share once the block has been
+    // through its positions (one barrier), so rebuilds of neighbouring points
+    // do not fall on one warp.  A full queue is rebuilt by the warp itself.
+    if (threadIdx.x == 0) sm.nq = 0;
+    __syncthreads();
+    for (int i0 = (bx * blockDim.x + threadIdx.x) & ~31; i0 < n; i0 += nbx * blockDim.x) {  // warp-uniform
+        const int i = i0 + lane;
+        bool need = false;
         if (i < n) {
             const int slot = sw[4 * (size_t)i];
             if (scnt[i] >= v.min_pts) {
                 v.rslot[slot] = uf_find(v.parent, v.sroot[i]);
             } else {
                 v.rslot[slot] = -1;
-                if (v.ntrack[slot] != 1) sm.queue[atomicAdd(&sm.nq, 1)] = i;
+                need = v.ntrack[slot] != 1;
             }
         }
-        __syncthreads();
-        const int nq = sm.nq;
-        for (int e = wib; e < nq; e += wpb) {
-            const int at = sm.queue[e];
-            const float4 ap = spt[at];
-            const int a = slot_of(ap);
-            int rs, re;
-            row_ranges<DIM, false, K>(v, v.table[cur], gen, v.skey[cur][at], lane, rs, re);
-            const int total = candidate_stream<Stencil<DIM, false, K>::kRows>(rs, re, 0, lane, rstart[wib], rpre[wib]);
-            int r = 0, nfound = 0;
-            for (int base = 0; base < total; base += 32) {
-                const int idx = base + lane;
-                bool nb = false;
-                int qs = -1;
-                if (idx < total) {
-                    const float4 q = spt[stream_pos(idx, r, rstart[wib], rpre[wib])];
-                    qs = slot_of(q);
-                    nb = qs != a && is_nbr<MODE, DIM>(v, ap, q, tally);
-                }
-                nfound = list_collect(nb, qs, nfound, v.list_cap, nbuf, lane);
-            }
-            list_store(v, a, nfound, nbuf, lane);
+        bool inline_rebuild = false;
+        if (need) {
+            const int at = atomicAdd(&sm.nq, 1);
+            if (at < kFlattenQueue)
+                sm.queue[at] = i;
+            else
+                inline_rebuild = true;
+        }
+        unsigned todo = __ballot_sync(kFull, inline_rebuild);
+        while (todo) {
+            rebuild_list<MODE, DIM, K>(v, i0 + __ffs(todo) - 1, cur, gen, lane, rstart[wib], rpre[wib], nbuf, tally);
+            todo &= todo - 1;
         }
     }
+    __syncthreads();
+    const int nq = min(sm.nq, kFlattenQueue);
+    for (int e = wib; e < nq; e += wpb)
+        rebuild_list<MODE, DIM, K>(v, sm.queue[e], cur, gen, lane, rstart[wib], rpre[wib], nbuf, tally);
     flush_stats(v, tally, 0, lane, 1);
 }
 
 template <int MODE, int DK>
-__global__ void __launch_bounds__(256) k_flatten(View v) {
+__global__ void __launch_bounds__(256, 6) k_flatten(View v) {
     __shared__ StreamSmem sm;
     flatten_body<MODE, DK>(v, blockIdx.x, gridDim.x, sm);
 }
@@ -1713,7 +1756,7 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
         reuse_body(sv, bx, nbx);
     } else if constexpr (PHASE == kBatchUnion) {
         __shared__ ClusterSmem sm;
-        union_body<MODE, DK>(sv, sm);
+        union_body<MODE, DK>(sv, sm, bx, nbx);
     } else if constexpr (PHASE == kBatchFlatten) {
         __shared__ StreamSmem sm;
         flatten_body<MODE, DK>(sv, bx, nbx, sm);

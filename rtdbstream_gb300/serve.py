@@ -5,11 +5,12 @@ next S points); the server keeps every admitted stream's window, grid, counts
 and forest resident in HBM and runs rounds back to back.  Each round takes the
 oldest pending request of every stream that has one, so requests that arrive
 while a round is on the GPU join a following round instead of waiting for a
-fixed batch.  Under a backlog rounds are pipelined: while one round runs on
-the GPU the host builds and queues the next once it holds at least as many
-requests (up to `depth` rounds in flight on the pool's CUDA stream, which
-keeps each stream's slides in order), so building a round does not leave the
-GPU idle.  Streams are admitted against an HBM budget and
+fixed batch.  With depth > 1 rounds are pipelined: while one round runs on
+the GPU the host builds and queues the next (up to `depth` rounds in flight
+on the pool's CUDA stream, which keeps each stream's slides in order), so
+building a round does not leave the GPU idle; each queued round also has a
+fixed cost, so at light load depth 1 (a round is formed when the previous
+one completes) gives the lower latency.  Streams are admitted against an HBM budget and
 wait for memory when it is exhausted; a stream that has had all its slides
 leaves and frees its memory.  Latency of a request = completion of its round
 (its CUDA event) - its arrival.
@@ -40,7 +41,7 @@ class ServedStream:
 
 
 class SlideServer:
-    def __init__(self, device: int = 0, hbm_budget_bytes: int = 120 * 10**9, stream: int = 0, depth: int = 2):
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 120 * 10**9, stream: int = 0, depth: int = 1):
         self.pool = Pool(device=device, hbm_budget_bytes=hbm_budget_bytes, use_graph=False, stream=stream)
         self.budget = hbm_budget_bytes
         self.depth = max(1, depth)
@@ -144,11 +145,7 @@ class SlideServer:
                                 self.admit_waits.append(done_t - first_req.pop(j))
             if len(inflight) < self.depth:
                 members = [i for i in active if self.streams[i].sid is not None]
-                # behind a running round only a round at least its size is
-                # queued: under a backlog the host's work overlaps the GPU's,
-                # at light load requests wait to form one round instead of
-                # queueing many small ones (each has a fixed cost)
-                if members and (not inflight or len(members) >= len(inflight[-1][1])):
+                if members:
                     ids, ptrs, arr = [], [], []
                     for i in members:
                         s = self.streams[i]

@@ -95,7 +95,7 @@ def test_budget_bound_results_match_streams_alone(torch_stream):
     streams = make_streams(20, seed=13)
     costs = [stream_bytes(make_params(sp.dim, sp.window, sp.stride, sp.eps, sp.min_pts)) for sp, _, _ in streams]
     budget = sum(sorted(costs)[-5:]) + 1        # any 5 streams fit, not all 20
-    srv = SlideServer(hbm_budget_bytes=budget, stream=torch_stream.cuda_stream, depth=3)
+    srv = SlideServer(hbm_budget_bytes=budget, stream=torch_stream.cuda_stream, depth=2)
     t, tgt = poisson_arrivals(rate=600.0, duration=0.4, n_streams=len(streams), seed=7)
     # every stream also gets 2..4 requests appended after the Poisson ones
     rng = np.random.default_rng(8)
