@@ -1296,11 +1296,10 @@ struct ClusterSmem {
     int home_root[kClusterThreads / 32][32];
     float4 home_pt[kClusterThreads / 32][32];
     int rstart[kClusterThreads / 32][kMaxRows], rpre[kClusterThreads / 32][kMaxRows + 1];
-    int seg_next;  // k_union: next item of the block's own segment
 };
 
 template <int MODE, int DK>
-__device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm, int bx, int nbx) {
+__device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
     constexpr int DIM = DK & 3, K = (DK >> 2) + 1;  // dimension, cells per Eps
     float4(&home_pt)[kClusterThreads / 32][32] = sm.home_pt;
     int(&rstart)[kClusterThreads / 32][kMaxRows] = sm.rstart;
@@ -1323,35 +1322,17 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm, int b
     volatile int* hint = v.sroot;
     Tally tally;
     int err = 0;
-    // Work split: the first 4/5 of the items in one contiguous segment per
-    // block, handed out an item at a time from a shared-memory counter (the
-    // block's warps take neighbouring cells, so candidate loads reuse L1);
-    // the rest from the stream's queue, v.grab consecutive items at a time,
-    // so blocks whose segment was cheap take more of it and uneven items do
-    // not leave warps idle at the end.
-    const int nstat = nitems - nitems / 5;
-    const int seg = (nstat + nbx - 1) / nbx;
-    const int s0 = min(bx * seg, nstat), s1 = min(s0 + seg, nstat);
-    if (threadIdx.x == 0) sm.seg_next = s0;
-    __syncthreads();
-    bool own = true;  // the block's segment may still hold items
+    // Warps take batches of v.grab consecutive work items (neighbouring
+    // cells: candidate loads reuse L1) from a counter, so uneven items do not
+    // leave warps idle at the end.
     int it1 = 0;
     for (int itx = nitems;;) {
         if (itx >= it1) {
-            int got = 0, from_seg = 0;
-            if (lane == 0) {
-                if (own) {
-                    got = atomicAdd(&sm.seg_next, 1);
-                    from_seg = got < s1 ? 1 : 0;
-                }
-                if (!from_seg) got = nstat + atomicAdd(&v.ctl->union_next, v.grab);
-            }
-            got = __shfl_sync(kFull, got, 0);
-            from_seg = __shfl_sync(kFull, from_seg, 0);
-            own = from_seg != 0;
-            if (got >= nitems) break;
-            itx = got;
-            it1 = from_seg ? got + 1 : min(got + v.grab, nitems);
+            int got = 0;
+            if (lane == 0) got = atomicAdd(&v.ctl->union_next, v.grab);
+            itx = __shfl_sync(kFull, got, 0);
+            if (itx >= nitems) break;
+            it1 = min(itx + v.grab, nitems);
         }
         const int2 item = v.items[itx++];
         const int start = item.x, len = item.y;
@@ -1423,7 +1404,7 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm, int b
 template <int MODE, int DK>
 __global__ void __launch_bounds__(kClusterThreads, 8) k_union(View v) {
     __shared__ ClusterSmem sm;
-    union_body<MODE, DK>(v, sm, blockIdx.x, gridDim.x);
+    union_body<MODE, DK>(v, sm);
 }
 
 // The neighbour list of the non-core point at sorted position `at`, from one
@@ -1756,7 +1737,7 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
         reuse_body(sv, bx, nbx);
     } else if constexpr (PHASE == kBatchUnion) {
         __shared__ ClusterSmem sm;
-        union_body<MODE, DK>(sv, sm, bx, nbx);
+        union_body<MODE, DK>(sv, sm);
     } else if constexpr (PHASE == kBatchFlatten) {
         __shared__ StreamSmem sm;
         flatten_body<MODE, DK>(sv, bx, nbx, sm);
