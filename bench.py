@@ -347,8 +347,8 @@ def measured_peak() -> tuple:
 
 def ncu_traffic(phase: str):
     """DRAM bytes per launch of the dominant kernel at W = 1M from the
-    committed ncu summary (profiles/ncu_traffic.json, a W = 250k capture
-    scaled by 4), or None."""
+    committed ncu summary (profiles/ncu_traffic.json, captured at the
+    bench's own size), or None."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(path) as f:
