@@ -223,6 +223,7 @@ size_t plan_layout(rtdbs_engine* e, std::vector<Part>& parts) {
     const size_t list_ints = (size_t)W * v.list_stride;
     const size_t track_ints = v.list_cap >= 0 ? (size_t)W : 0;
     v.nlist = v.ntrack = v.rslot = v.damaged = nullptr;
+    v.sprev[0] = v.sprev[1] = nullptr;
     parts = {
         {(void**)&v.ring, sizeof(float4) * W},
         {(void**)&v.kslot, sizeof(unsigned long long) * W},
@@ -243,6 +244,8 @@ size_t plan_layout(rtdbs_engine* e, std::vector<Part>& parts) {
         {(void**)&v.ntrack, sizeof(int) * track_ints},
         {(void**)&v.rslot, sizeof(int) * track_ints},
         {(void**)&v.damaged, sizeof(int) * track_ints},
+        {(void**)&v.sprev[0], sizeof(int) * track_ints},
+        {(void**)&v.sprev[1], sizeof(int) * track_ints},
         {(void**)&v.nsort, sizeof(unsigned long long) * C},
         {(void**)&v.xsort, sizeof(unsigned long long) * C},
         {(void**)&v.nword, sizeof(unsigned long long) * C},
@@ -266,7 +269,7 @@ int allocate(rtdbs_engine* e) {
     e->dev_bytes = total;
     char* base = static_cast<char*>(e->dev_block);
     for (auto& q : parts) {
-        *q.ptr = base;
+        *q.ptr = q.bytes ? base : nullptr;  // a buffer this stream does not use stays null
         base += align_up(q.bytes, 256);
     }
     CUDA_TRY(cudaMemsetAsync(v.table[0], 0, sizeof(ulonglong2) * P, e->stream));
@@ -554,7 +557,7 @@ int rtdbs_cluster(rtdbs_engine* e, int32_t* label, int32_t* cluster_id, int on_d
     if (!e->loaded) return fail(RTDBS_ERR_STATE, "rtdbs_load_window must come first");
     DeviceGuard guard(e->device);
     CUDA_TRY(guard.err);
-    CUDA_TRY(rtdbs::launch_cluster(e->v, e->p.precision, 0, e->stream));
+    CUDA_TRY(rtdbs::launch_cluster(e->v, e->p.precision, 0, e->stream, true));
     int rc = copy_out(e, label, cluster_id, on_device);
     if (rc == RTDBS_OK) rc = fetch_ctl_and_sync(e);
     return rc;
@@ -614,9 +617,9 @@ int rtdbs_get_stats(rtdbs_engine* e, rtdbs_stats* s) {
     s->device_bytes = (int64_t)e->dev_bytes;
     const int nchunks = (e->p.stride + e->chunk - 1) / e->chunk;
     s->chunks_per_slide = nchunks;
-    // sort phase = 2 kernels; with neighbour lists the union phase adds the
-    // two forest-reuse passes
-    s->launches_per_slide = nchunks * (rtdbs::kChunkPhases + 1) + 4 + (e->v.list_cap >= 0 ? 1 : 0);
+    // per chunk 7 kernels (the sort phase is 2); then union, flatten and
+    // label (or border)
+    s->launches_per_slide = nchunks * (rtdbs::kChunkPhases + 1) + 3;
     return RTDBS_OK;
 }
 
@@ -839,7 +842,9 @@ int pool_build_shape(rtdbs_pool* p, const std::vector<int>& ids) {
         for (int ph = 0; ph < rtdbs::kBatchChunkPhases; ++ph) add_launches(ph, items);
     }
     for (auto& it : all_items) it.c = 0;  // cluster phases size by W only
-    for (int ph = rtdbs::kBatchDamage; ph <= rtdbs::kBatchLabel; ++ph) add_launches(ph, all_items);
+    // (no damage or reuse launch: the ingest and the decrement mark the lost
+    // cores, the merge and the increment set the start hints)
+    for (int ph = rtdbs::kBatchUnion; ph <= rtdbs::kBatchLabel; ++ph) add_launches(ph, all_items);
     if (img.size() > p->tables_cap) {
         // (cudaFree waits for the rounds that still read the old buffer)
         if (p->d_tables) cudaFree(p->d_tables);

@@ -24,6 +24,8 @@
 //   damaged i32[W]        per previous root: the component lost a core this slide
 //   ntrack i32[W]         1: the slot's list is exact; 0: not kept (core, or
 //                         rebuilt at the end of the slide)
+//   sprev  i32[2][W]      per sorted position: the point's root at the last
+//                         clustering (-1: not core), carried by the merges
 //   chunk scratch: sort words, expired points.
 #pragma once
 
@@ -127,6 +129,10 @@ struct View {
     int* damaged;                // per old root slot: its component lost a core this
                                  // slide (0 outside the union phase)
     int* ntrack;                 // per slot: 1 list exact, 0 not kept
+    int* sprev[2];               // per sorted position (with the sorted buffers): the
+                                 // point's root at the last clustering, -1 if it was not
+                                 // core (or not there); carried by the merges for forest
+                                 // reuse; null without neighbour lists
     unsigned long long* nsort;   // chunk sort words in (key << 14 | offset)
     unsigned long long* xsort;
     unsigned long long* nword;   // sorted
@@ -167,7 +173,9 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
 cudaError_t launch_chunk_step(const View& v, int precision, int j, int c, int init,
                               int staging_offset, cudaStream_t s, cudaStream_t side = nullptr,
                               cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
-cudaError_t launch_cluster(const View& v, int precision, int advance, cudaStream_t s);
+// fresh_hints: start the union from fresh hints and forest (no reuse), for a
+// clustering of the window as it stands rather than after a slide.
+cudaError_t launch_cluster(const View& v, int precision, int advance, cudaStream_t s, bool fresh_hints = false);
 cudaError_t launch_counts_by_slot(const View& v, int* nn_by_slot, cudaStream_t s);
 cudaError_t configure_kernels();
 

@@ -526,6 +526,63 @@ __device__ __forceinline__ void list_store(const View& v, int a, int nfound, con
 
 // ------------------------------------------------------------------- kernels
 
+// ------------------------------------------------------ forest reuse
+// A component of the previous clustering that lost no core this slide (no
+// core expired, no core fell below MinPts) is still connected: all its
+// cores and the edges between them remain.  Its cores start the union as
+// one set under the old root (still its minimum slot), with that root as
+// their hint, so pairs inside it are skipped by hint equality; every other
+// core starts as a singleton.  The union still visits every core pair, so
+// merges through new cores and splits of damaged components come out exactly
+// as in a union from scratch.  Used with neighbour lists, where k_border
+// leaves the previous labels and ids by slot and resets the forest.
+//
+// No pass of its own: the old root of every core lost this slide is marked
+// damaged as the loss happens -- an expired core in the ingest, a core whose
+// count falls below MinPts in the decrement (a count that falls below and
+// rises again within the slide only marks a component that did not need it;
+// it is then re-united from scratch, still exactly) -- and the merge, which
+// rewrites every position, starts each core under its old root or alone
+// (start_hint); the increment then sets the hints of new points and of points
+// it lifts to MinPts.  label/cid hold the previous clustering until the
+// border pass ends the slide.
+
+// Reuse is skipped for 15 slides after a slide where fewer than 1 in 16 of
+// the window's points joined a reused component (streams whose expiries
+// touch every cluster), then tried again.
+constexpr int kReuseRetry = 15;
+
+__device__ __forceinline__ bool damage_on(const View& v) {
+    return v.list_cap >= 0 && v.ctl->prev_ok && v.ctl->reuse_skip <= 0;
+}
+
+// The slide's new slots: [base, base + S).
+__device__ __forceinline__ bool slot_is_new(const View& v, int s) {
+    const int base = (int)(v.ctl->slide % v.units) * v.S;
+    return s >= base && s < base + v.S;
+}
+
+// Root hint a position starts the union with: -1 for a non-core point; the
+// old root `prev` of a core of an intact component (the root the point had
+// at the last clustering, carried with it by the merges; -1 for a point that
+// was not core then); else its own slot.  Counts 1 in `reused` for a
+// reused core.  The parents need no change: the union and the flatten only
+// ever start from a point's hint, and the border pass leaves every parent at
+// its own slot.
+__device__ __forceinline__ int start_hint(const View& v, int s, int cnt, int prev, bool reuse,
+                                          unsigned& reused) {
+    if (cnt < v.min_pts) return -1;
+    if (reuse && prev >= 0 && !v.damaged[prev]) {
+        ++reused;
+        return prev;
+    }
+    return s;
+}
+
+__device__ __forceinline__ void mark_damage(const View& v, int slot) {
+    if (v.label[slot] == 0) v.damaged[v.cid[slot]] = 1;
+}
+
 // New points of chunk j -> ring slots [el, el+c): float4 + cell key; the
 // points they replace are kept for the decrement pass.
 __device__ __forceinline__ void ingest_body(const View& v, int j, int c, int init, int stg_off,
@@ -537,6 +594,7 @@ __device__ __forceinline__ void ingest_body(const View& v, int j, int c, int ini
     if (!init) {
         v.xpt[k] = v.ring[slot];
         v.xsort[k] = (v.kslot[slot] << kOffBits) | (unsigned long long)k;
+        if (damage_on(v)) mark_damage(v, slot);  // an expired core
     }
     const float* p = input + (size_t)(stg_off + k) * v.dim;
     const float x = p[0];
@@ -752,6 +810,7 @@ __device__ __forceinline__ void decr_g(const View& v, int j, int c, int bx, Stre
     const float4* spt = v.spt[old];
     int* scnt = v.scnt[old];
     const bool lists = v.list_cap >= 0;
+    const bool damage = damage_on(v);
     const int xs = slot_of(xp);
     Tally tally;
     int r = 0;
@@ -767,12 +826,20 @@ __device__ __forceinline__ void decr_g(const View& v, int j, int c, int bx, Stre
         const int qs0 = slot_of(q0), qs1 = slot_of(q1);
         float d0, d1;
         sqdist32x2<DIM>(xp, q0, q1, d0, d1);
+        // counts only fall here: one read below MinPts cannot cross it, so
+        // only the others need the count the decrement leaves
         if ((qs0 < el || qs0 >= el + c) && nbr_decide<MODE, DIM>(v, d0, xp, q0, tally)) {
-            atomicSub(&scnt[pos0], 1);
+            if (!damage || cnt0 < v.min_pts)
+                atomicSub(&scnt[pos0], 1);
+            else if (atomicSub(&scnt[pos0], 1) == v.min_pts)
+                mark_damage(v, qs0);  // a core falls below MinPts
             if (lists && cnt0 < v.min_pts && v.ntrack[qs0] == 1) list_remove(v, qs0, xs);
         }
         if (two && (qs1 < el || qs1 >= el + c) && nbr_decide<MODE, DIM>(v, d1, xp, q1, tally)) {
-            atomicSub(&scnt[pos1], 1);
+            if (!damage || cnt1 < v.min_pts)
+                atomicSub(&scnt[pos1], 1);
+            else if (atomicSub(&scnt[pos1], 1) == v.min_pts)
+                mark_damage(v, qs1);
             if (lists && cnt1 < v.min_pts && v.ntrack[qs1] == 1) list_remove(v, qs1, xs);
         }
     }
@@ -877,6 +944,11 @@ __device__ __forceinline__ void merge_body(const View& v, int j, int c, int init
     // a fresh union-find forest: with neighbour lists k_border resets it by
     // slot at the end of every clustering, so only the first window needs it
     const bool reset_parent = init || v.list_cap < 0;
+    // forest reuse: the hints of the slide's last chunk step stand (every
+    // loss of the slide is marked by then), so only that step counts reuses
+    const bool reuse = !init && damage_on(v);
+    const bool last_step = j * v.chunk + c >= v.S;
+    unsigned reused = 0;
     if (bx == 0 && tid == 0) {
         v.ctl->nocc[dst] = n_new;
         v.ctl->nitems = 0;
@@ -902,6 +974,8 @@ __device__ __forceinline__ void merge_body(const View& v, int j, int c, int init
     unsigned long long* dkey = v.skey[dst];
     float4* dpt = v.spt[dst];
     int* dcnt = v.scnt[dst];
+    const int* oprev = v.sprev[src];
+    int* dprev = v.sprev[dst];
 
     // tile bounds among the new / expired words: warps 0, 1, 2 search at once
     {
@@ -982,9 +1056,16 @@ __device__ __forceinline__ void merge_body(const View& v, int j, int c, int init
         }
         dkey[o] = tkey[i];
         dpt[o] = opt[ts + i];
-        dcnt[o] = ocnt[ts + i];
-        v.sroot[o] = s;
+        const int cnt = ocnt[ts + i];
+        dcnt[o] = cnt;
+        const int prev = oprev ? oprev[ts + i] : -1;
+        if (dprev) dprev[o] = prev;
+        v.sroot[o] = start_hint(v, s, cnt, prev, reuse, reused);
         if (reset_parent) v.parent[s] = s;
+    }
+    if (last_step) {
+        reused = __reduce_add_sync(kFull, reused);
+        if ((tid & 31) == 0 && reused) atomicAdd(&v.ctl->reused, (int)reused);
     }
     // new entries of this tile
     for (int q = jt0 + tid; q < jt1; q += kMergeThreads) {
@@ -1007,7 +1088,8 @@ __device__ __forceinline__ void merge_body(const View& v, int j, int c, int init
         dkey[o] = key;
         dpt[o] = v.ring[slot];
         dcnt[o] = 0;
-        v.sroot[o] = slot;
+        if (dprev) dprev[o] = -1;
+        v.sroot[o] = -1;  // the increment sets the count and the hint
         if (reset_parent) v.parent[slot] = slot;
         // the chunk's order, for the slide that expires it (every reader of
         // the expired order of these slots ran before this pass)
@@ -1164,7 +1246,12 @@ __device__ __forceinline__ void incr_g(const View& v, int j, int c, int init, in
                 ++count;
                 nb[u] = true;
                 if (qs[u] < el || qs[u] >= el + c) {
-                    atomicAdd(&scnt[pos[u]], 1);
+                    // counts only rise here: one read below MinPts may be the
+                    // increment that makes the point core, which sets its hint
+                    if (cnt[u] >= v.min_pts)
+                        atomicAdd(&scnt[pos[u]], 1);
+                    else if (atomicAdd(&scnt[pos[u]], 1) == v.min_pts - 1)
+                        v.sroot[pos[u]] = qs[u];  // now core
                     if (lists && cnt[u] < v.min_pts && v.ntrack[qs[u]] == 1) list_append(v, qs[u], aslot);
                 }
             }
@@ -1182,10 +1269,12 @@ __device__ __forceinline__ void incr_g(const View& v, int j, int c, int init, in
     }
     int err = 0;
     if (gl == 0 && has) {
-        if (mypos >= 0)
+        if (mypos >= 0) {
             scnt[mypos] = count;
-        else
+            v.sroot[mypos] = count >= v.min_pts ? aslot : -1;
+        } else {
             err = kErrChunk;
+        }
     }
     flush_query_max<G>(v, tally.tests, lane);
     flush_stats(v, tally, err, lane, 0);
@@ -1203,86 +1292,26 @@ __device__ __forceinline__ void incr_body(const View& v, int j, int c, int init,
 }
 
 template <int MODE, int DK>
-__global__ void __launch_bounds__(256) k_incr(View v, int j, int c, int init) {
+__global__ void __launch_bounds__(256, 5) k_incr(View v, int j, int c, int init) {
     __shared__ StreamSmem sm;
     incr_body<MODE, DK>(v, j, c, init, blockIdx.x, sm);
 }
 
-// ------------------------------------------------------ forest reuse
-// A component of the previous clustering that lost no core this slide (no
-// core expired, no core fell below MinPts) is still connected: all its
-// cores and the edges between them remain.  Its cores start the union as
-// one set under the old root (still its minimum slot), with that root as
-// their hint, so pairs inside it are skipped by hint equality; every other
-// core starts as a singleton.  The union still visits every core pair, so
-// merges through new cores and splits of damaged components come out exactly
-// as in a union from scratch.  Used with neighbour lists, where k_border
-// leaves the previous labels and ids by slot and resets the forest.
-
-// Reuse is skipped for 15 slides after a slide where fewer than 1 in 16 of
-// the window's points joined a reused component (streams whose expiries
-// touch every cluster), then tried again.
-constexpr int kReuseRetry = 15;
-
-// The slide's new slots: [base, base + S).
-__device__ __forceinline__ bool slot_is_new(const View& v, int s) {
-    const int base = (int)(v.ctl->slide % v.units) * v.S;
-    return s >= base && s < base + v.S;
-}
-
-// Marks the old root of every core lost this slide: expired cores (slots of
-// the new points, read before the border pass overwrites them) and cores
-// now below MinPts.
-__device__ __forceinline__ void damage_body(const View& v, int bx, int nbx) {
-    if (!v.ctl->prev_ok || v.ctl->reuse_skip > 0) return;
-    const int cur = (int)(v.ctl->b & 1);
-    const int n = v.ctl->nocc[cur];
-    const int* scnt = v.scnt[cur];
-    const int* sw = reinterpret_cast<const int*>(v.spt[cur]) + 3;  // .w = slot
-    const int base = (int)(v.ctl->slide % v.units) * v.S;
-    for (int i = bx * blockDim.x + threadIdx.x; i < n + v.S; i += nbx * blockDim.x) {
-        int s;
-        if (i < n) {
-            if (scnt[i] >= v.min_pts) continue;
-            s = sw[4 * (size_t)i];
-            if (slot_is_new(v, s)) continue;
-        } else {
-            s = base + (i - n);  // an expired point's slot
-        }
-        if (v.label[s] == 0) v.damaged[v.cid[s]] = 1;
-    }
-}
-
-// Marks every non-core position's hint -1 (the union then tells cores from
-// their hint alone), and, with neighbour lists, lets the cores of intact
-// components join their old root (parent and hint).
-__device__ __forceinline__ void reuse_body(const View& v, int bx, int nbx) {
-    const bool reuse_on = v.list_cap >= 0 && v.ctl->prev_ok && v.ctl->reuse_skip <= 0;
+// Fresh start hints without reuse (-1 for a non-core position, its own
+// slot for a core) and a fresh forest, for a clustering of the window as it
+// stands (rtdbs_cluster), whose hints may hold the last union's roots.
+__global__ void k_hints(View v) {
     const int cur = (int)(v.ctl->b & 1);
     const int n = v.ctl->nocc[cur];
     const int* scnt = v.scnt[cur];
     const int* sw = reinterpret_cast<const int*>(v.spt[cur]) + 3;
-    unsigned reused = 0;
-    for (int i = bx * blockDim.x + threadIdx.x; i < n; i += nbx * blockDim.x) {
-        if (scnt[i] < v.min_pts) {
-            v.sroot[i] = -1;
-            continue;
-        }
-        if (!reuse_on) continue;
+    if (blockIdx.x == 0 && threadIdx.x == 0) v.ctl->prev_ok = 0;  // no reuse to judge (read by k_border)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int s = sw[4 * (size_t)i];
-        if (v.label[s] != 0 || slot_is_new(v, s)) continue;
-        const int r = v.cid[s];
-        if (v.damaged[r]) continue;
-        v.parent[s] = r;
-        v.sroot[i] = r;
-        ++reused;
+        v.sroot[i] = scnt[i] >= v.min_pts ? s : -1;
+        v.parent[s] = s;
     }
-    reused = __reduce_add_sync(kFull, reused);
-    if ((threadIdx.x & 31) == 0 && reused) atomicAdd(&v.ctl->reused, (int)reused);
 }
-
-__global__ void k_damage(View v) { damage_body(v, blockIdx.x, gridDim.x); }
-__global__ void k_reuse(View v) { reuse_body(v, blockIdx.x, gridDim.x); }
 
 // Union of every core-core neighbour pair, each unordered pair once (the
 // candidate's sorted position is above the home point's).  A candidate's
@@ -1315,10 +1344,11 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
     const unsigned long long* skey = v.skey[cur];
     const ulonglong2* T = v.table[cur];
     int* parent = v.parent;
-    // Root hints by sorted position (an ancestor of the point; the merge sets
-    // each to the point's own slot, k_reuse marks non-core points -1, so the
-    // hint alone tells a core): coalesced with the candidate loads, and
-    // refreshed as roots are found, so find walks stay short.
+    // Root hints by sorted position (an ancestor of the point: its own slot
+    // or the old root of its intact component; -1 for a non-core point, so
+    // the hint alone tells a core; set by the merge and the increment, see
+    // start_hint): coalesced with the candidate loads, and refreshed as roots
+    // are found, so find walks stay short.
     volatile int* hint = v.sroot;
     Tally tally;
     int err = 0;
@@ -1471,9 +1501,12 @@ __device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx, Str
         if (i < n) {
             const int slot = sw[4 * (size_t)i];
             if (scnt[i] >= v.min_pts) {
-                v.rslot[slot] = uf_find(v.parent, v.sroot[i]);
+                const int root = uf_find(v.parent, v.sroot[i]);
+                v.rslot[slot] = root;
+                v.sprev[cur][i] = root;  // the next slide's reuse reads it by position
             } else {
                 v.rslot[slot] = -1;
+                v.sprev[cur][i] = -1;
                 need = v.ntrack[slot] != 1;
             }
         }
@@ -1636,7 +1669,7 @@ __device__ __forceinline__ void border_body(const View& v, int advance, int bx, 
     }
     if (bx == 0 && threadIdx.x == 0) {
         v.ctl->union_next = 0;                // the next clustering's queue; not read here
-        // k_damage / k_reuse of this clustering are done: judge the reuse
+        // the reuse of this clustering is counted: judge it
         // (not after a fresh window, which had no previous forest)
         if (v.ctl->reuse_skip > 0)
             v.ctl->reuse_skip -= 1;
@@ -1731,10 +1764,6 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
     } else if constexpr (PHASE == kBatchIncrement) {
         __shared__ StreamSmem sm;
         incr_body<MODE, DK>(sv, it.j, it.c, 0, bx, sm);
-    } else if constexpr (PHASE == kBatchDamage) {
-        if (sv.list_cap >= 0) damage_body(sv, bx, nbx);
-    } else if constexpr (PHASE == kBatchReuse) {
-        reuse_body(sv, bx, nbx);
     } else if constexpr (PHASE == kBatchUnion) {
         __shared__ ClusterSmem sm;
         union_body<MODE, DK>(sv, sm);
@@ -1835,12 +1864,6 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
             }
             [[fallthrough]];
         case kPhaseUnion: {
-            if (phase == kPhaseUnion) {  // (the label phase without lists falls through)
-                const int sms0 = g_num_sms > 0 ? g_num_sms : 152;
-                const int rb = max(1, min(sms0 * 8, (v.W + 255) / 256));
-                if (v.list_cap >= 0) k_damage<<<rb, 256, 0, s>>>(v);
-                k_reuse<<<rb, 256, 0, s>>>(v);
-            }
             const int sms = g_num_sms > 0 ? g_num_sms : 152;
             const int per_block = kClusterThreads / 32;
             const int need = (v.max_items + per_block - 1) / per_block;  // one warp per item at most
@@ -1883,8 +1906,13 @@ cudaError_t launch_chunk_step(const View& v, int precision, int j, int c, int in
     return cudaSuccess;
 }
 
-cudaError_t launch_cluster(const View& v, int precision, int advance, cudaStream_t s) {
+cudaError_t launch_cluster(const View& v, int precision, int advance, cudaStream_t s, bool fresh_hints) {
     cudaError_t e = cudaSuccess;
+    if (fresh_hints) {
+        const int sms = g_num_sms > 0 ? g_num_sms : 152;
+        k_hints<<<max(1, min(sms * 8, (v.W + 255) / 256)), 256, 0, s>>>(v);
+        e = cudaGetLastError();
+    }
     for (int ph = kPhaseUnion; ph <= kPhaseLabel && e == cudaSuccess; ++ph)
         e = launch_phase(ph, v, precision, 0, 0, 0, 0, advance, s);
     return e;
@@ -1912,8 +1940,8 @@ int batch_blocks(int phase, const View& v, int c) {
         case kBatchIncrement: return (c * v.qlanes + 255) / 256;
         case kBatchMerge: return (v.W + kMergeTile - 1) / kMergeTile;
         case kBatchBuild: return (v.W + kBuildThreads - 1) / kBuildThreads;
-        case kBatchDamage: return v.list_cap >= 0 ? max(1, min(1024, (v.W + 2047) / 2048)) : 0;
-        case kBatchReuse: return max(1, min(1024, (v.W + 2047) / 2048));
+        case kBatchDamage: return 0;  // marked in the ingest and the decrement
+        case kBatchReuse: return 0;  // start hints set by the merge and the increment
         case kBatchUnion: return max(1, min(1024, (v.W + 1023) / 1024));  // persistent, queue-fed
         case kBatchLabel:
             if (v.list_cap >= 0) return max(1, min(1024, (v.W + 1023) / 1024));  // k_border
@@ -1967,8 +1995,8 @@ cudaError_t launch_batch(int phase, int prec, int dim, const BatchLaunch& L, int
         case kBatchBuild: k_batch<kBatchBuild, 0, 0><<<total_blocks, t, 0, s>>>(L); break;
         case kBatchDecrement: RTDBS_BATCH_MD(kBatchDecrement, total_blocks, t, s); break;
         case kBatchIncrement: RTDBS_BATCH_MD(kBatchIncrement, total_blocks, t, s); break;
-        case kBatchDamage: k_batch<kBatchDamage, 0, 0><<<total_blocks, t, 0, s>>>(L); break;
-        case kBatchReuse: k_batch<kBatchReuse, 0, 0><<<total_blocks, t, 0, s>>>(L); break;
+        case kBatchDamage: break;  // no kernel: marked in the ingest and the decrement
+        case kBatchReuse: break;  // no kernel: start hints set by the merge and the increment
         case kBatchUnion: RTDBS_BATCH_MD(kBatchUnion, total_blocks, t, s); break;
         case kBatchFlatten: RTDBS_BATCH_MD(kBatchFlatten, total_blocks, t, s); break;
         case kBatchLabel: RTDBS_BATCH_MD(kBatchLabel, total_blocks, t, s); break;
