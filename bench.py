@@ -11,8 +11,12 @@ value  -- device-resident: the whole stream sits in HBM before timing; each
           step is rtdbs_slide_async (D2D of the S new points into the engine,
           one CUDA-graph replay); CUDA events on the engine's stream around each
           step; L2 flushed (256 MB write) between steps outside the events.
-e2e    -- rtdbs_slide with pinned host buffers: H2D of S points, the slide,
-          D2H of label[W] and cluster_id[W], host wall clock per call.
+e2e    -- through the host-buffer API with pinned buffers, every step the H2D
+          of S points, the slide and the D2H of label[W] and cluster_id[W]:
+          rtdbs_slide_pipelined (one slide in flight: each call returns the
+          previous slide's result), host wall clock over all steps and the
+          final sync -- the value; and rtdbs_slide (synchronous, L2 flushed
+          before each call), host wall clock per call -- its latency.
 With N > 1 (torchrun), every rank slides its own stream (seed + rank): the
 path shards by stream with no collective (weak scaling).
 
@@ -372,7 +376,7 @@ def run_ours(args) -> None:
     from rtdbstream_gb300 import Engine
 
     W, S = SPEC.window, SPEC.stride
-    total_steps = args.warmup + args.steps + args.e2e_steps + args.profile_steps
+    total_steps = args.warmup + args.steps + 2 * args.e2e_steps + args.profile_steps
     pts = walker_stream(W + total_steps * S, seed=1 + rank)
     d_pts = torch.from_numpy(pts).to(f"cuda:{dev}")
     # One dedicated stream for the engine, the timing events and the L2 flush
@@ -425,7 +429,22 @@ def run_ours(args) -> None:
         eng.slide(h_pts[W + step * S: W + (step + 1) * S], h_lab, h_cid)
         e2e_s.append(time.perf_counter() - t0)
         step += 1
-    e2e_value = S / statistics.mean(e2e_s) if e2e_s else None
+    e2e_sync_value = S / statistics.mean(e2e_s) if e2e_s else None
+    # pipelined: one slide in flight, outputs alternate between two pinned
+    # buffer pairs (a pair is free again once the call after next returns);
+    # the engine's ~220 MB working set per slide exceeds L2, so no flush
+    outs = [(torch.empty(W, dtype=torch.int32).pin_memory().numpy(),
+             torch.empty(W, dtype=torch.int32).pin_memory().numpy()) for _ in range(2)]
+    e2e_value = None
+    if args.e2e_steps:
+        eng.sync()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.e2e_steps):
+            eng.slide_pipelined(h_pts[W + step * S: W + (step + 1) * S], *outs[k % 2])
+            step += 1
+        eng.sync()
+        e2e_value = S * args.e2e_steps / (time.perf_counter() - t0)
 
     # per-phase device times (direct launches bracketed by events) and the
     # counters of the same slides
@@ -470,7 +489,9 @@ def run_ours(args) -> None:
         "latency_ms": {"p50": float(np.percentile(per_ms, 50)), "p99": float(np.percentile(per_ms, 99))},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": S * 3 * 4,
                 "d2h_bytes_per_step": 2 * W * 4,
-                "latency_ms_p50": 1000 * float(np.percentile(e2e_s, 50)) if e2e_s else None},
+                "api": "rtdbs_slide_pipelined, pinned host buffers, one slide in flight",
+                "synchronous": {"api": "rtdbs_slide", "value": e2e_sync_value,
+                                "latency_ms_p50": 1000 * float(np.percentile(e2e_s, 50)) if e2e_s else None}},
         "gpu_launches": args.steps * st["launches_per_slide"],
         "roofline": roofline,
         "cpu_baseline": cpu,

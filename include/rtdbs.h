@@ -189,6 +189,20 @@ RTDBS_API int rtdbs_slide(rtdbs_engine* engine, const float* new_points, int32_t
 RTDBS_API int rtdbs_slide_async(rtdbs_engine* engine, const float* d_new_points, int32_t* d_label,
                       int32_t* d_cluster_id);
 
+/* One slide with host buffers, pipelined: enqueues the slide (new points in,
+ * label[W] and cluster_id[W] out, as rtdbs_slide) and returns once the
+ * previous pipelined slide is complete, so the host prepares slide k+1 while
+ * slide k runs.  On return the previous call's label/cluster_id hold its
+ * result and its new_points may be reused; this call's three buffers stay in
+ * use until the next pipelined call, or any synchronising call, returns.
+ * Pinned host buffers keep the copies asynchronous (pageable memory makes
+ * them synchronous).  A device bound hit by a slide is reported by the call
+ * that completes it.  The reference's loop reads every slide's result before
+ * taking the next stride (src/dbscan/dbscan.cpp:2276-2362); this is the same
+ * loop with one slide in flight. */
+RTDBS_API int rtdbs_slide_pipelined(rtdbs_engine* engine, const float* new_points, int32_t* label,
+                                    int32_t* cluster_id);
+
 /* Waits for the engine's stream; reports RTDBS_ERR_DEVICE if a device bound
  * was hit by any work since the previous check. */
 RTDBS_API int rtdbs_sync(rtdbs_engine* engine);

@@ -179,6 +179,11 @@ struct rtdbs_engine {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double cell_side = 0.0;
+    // rtdbs_slide_pipelined: the end of the last two pipelined slides, and
+    // whether one is still in flight
+    cudaEvent_t ev_pipe[2] = {nullptr, nullptr};
+    int pipe_next = 0;
+    bool pipe_pending = false;
 };
 
 namespace {
@@ -349,6 +354,7 @@ int copy_out(rtdbs_engine* e, int32_t* label, int32_t* cid, int on_device) {
 int fetch_ctl_and_sync(rtdbs_engine* e) {
     CUDA_TRY(cudaMemcpyAsync(e->h_ctl, e->v.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->stream));
     CUDA_TRY(cudaStreamSynchronize(e->stream));
+    e->pipe_pending = false;  // everything queued, pipelined slides included, is done
     return check_device_error(e);
 }
 
@@ -461,6 +467,8 @@ int rtdbs_destroy(rtdbs_engine* e) {
     if (e->h_ctl) cudaFreeHost(e->h_ctl);
     if (e->side) cudaStreamDestroy(e->side);
     if (e->ev_fork) cudaEventDestroy(e->ev_fork);
+    for (auto& ev : e->ev_pipe)
+        if (ev) cudaEventDestroy(ev);
     if (e->ev_join) cudaEventDestroy(e->ev_join);
     if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
     delete e;
@@ -543,6 +551,30 @@ int rtdbs_slide_async(rtdbs_engine* e, const float* d_new_points, int32_t* d_lab
     if (rc == RTDBS_OK) rc = run_slide(e);
     if (rc == RTDBS_OK && (d_label || d_cluster_id)) rc = copy_out(e, d_label, d_cluster_id, 1);
     return rc;
+}
+
+int rtdbs_slide_pipelined(rtdbs_engine* e, const float* new_points, int32_t* label, int32_t* cluster_id) {
+    if (!e || !new_points) return fail(RTDBS_ERR_INVALID, "engine/new_points is NULL");
+    if (!e->loaded) return fail(RTDBS_ERR_STATE, "rtdbs_load_window must come first");
+    DeviceGuard guard(e->device);
+    CUDA_TRY(guard.err);
+    for (auto& ev : e->ev_pipe)
+        if (!ev) CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    int rc = copy_in(e, new_points, e->p.stride, 0);
+    if (rc == RTDBS_OK) rc = run_slide(e);
+    if (rc == RTDBS_OK) rc = copy_out(e, label, cluster_id, 0);
+    if (rc != RTDBS_OK) return rc;
+    // the control block follows the slide's outputs, so the previous slide's
+    // error bits are on the host once its event has passed
+    CUDA_TRY(cudaMemcpyAsync(e->h_ctl, e->v.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->stream));
+    const int cur = e->pipe_next;
+    CUDA_TRY(cudaEventRecord(e->ev_pipe[cur], e->stream));
+    e->pipe_next = cur ^ 1;
+    const bool wait_prev = e->pipe_pending;
+    e->pipe_pending = true;
+    if (!wait_prev) return RTDBS_OK;
+    CUDA_TRY(cudaEventSynchronize(e->ev_pipe[cur ^ 1]));
+    return check_device_error(e);
 }
 
 int rtdbs_sync(rtdbs_engine* e) {
@@ -823,10 +855,18 @@ int pool_build_shape(rtdbs_pool* p, const std::vector<int>& ids) {
             plan.push_back({ph, g.first, g.second, items_off, prefix_off, (int)sel.size(), prefix.back(), max_c});
         }
     };
+    // Launch order: largest windows first, so the blocks of the smallest
+    // streams fill the last wave of each launch (the packed input keeps the
+    // caller's order).
+    std::vector<int> ord(n);
+    for (int i = 0; i < n; ++i) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+        return p->eng[ids[a]]->p.window > p->eng[ids[b]]->p.window;
+    });
     std::vector<BatchItem> all_items;
     for (int j = 0; j < maxchunks; ++j) {
         std::vector<BatchItem> items;
-        for (int i = 0; i < n; ++i) {
+        for (int i : ord) {
             const rtdbs_engine* e = p->eng[ids[i]];
             const int S = e->p.stride, C = e->chunk;
             if (j * C >= S) continue;

@@ -30,6 +30,7 @@ FLAG_NO_GRAPH = 1
 EXPORTED_SYMBOLS = (
     "rtdbs_abi_version", "rtdbs_status_string", "rtdbs_last_error", "rtdbs_params_init",
     "rtdbs_create", "rtdbs_destroy", "rtdbs_load_window", "rtdbs_slide", "rtdbs_slide_async",
+    "rtdbs_slide_pipelined",
     "rtdbs_sync", "rtdbs_cluster", "rtdbs_get_counts", "rtdbs_device_outputs", "rtdbs_get_stats",
     "rtdbs_slide_profiled", "rtdbs_cluster_window_noalloc",
     "rtdbs_stream_bytes", "rtdbs_pool_params_init", "rtdbs_pool_create", "rtdbs_pool_destroy",
@@ -113,6 +114,7 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     L.rtdbs_load_window.argtypes = [vp, vp, ctypes.c_int]
     L.rtdbs_slide.argtypes = [vp, vp, vp, vp]
     L.rtdbs_slide_async.argtypes = [vp, vp, vp, vp]
+    L.rtdbs_slide_pipelined.argtypes = [vp, vp, vp, vp]
     L.rtdbs_sync.argtypes = [vp]
     L.rtdbs_cluster.argtypes = [vp, vp, vp, ctypes.c_int]
     L.rtdbs_get_counts.argtypes = [vp, vp, ctypes.c_int]
@@ -222,6 +224,21 @@ class Engine:
         if label is None:
             return lab.copy(), cid.copy()
         return lab, cid
+
+    def slide_pipelined(self, new_points: np.ndarray, label: np.ndarray, cluster_id: np.ndarray) -> None:
+        """One slide with host buffers, one slide in flight: returns once the
+        previous pipelined slide is complete (its label/cluster_id arrays then
+        hold its result); this call's arrays stay in use until the next
+        pipelined call or sync().  Pinned arrays keep the copies asynchronous."""
+        a = new_points
+        if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous
+                and a.shape == (self.stride_size, self.dim)):
+            raise ValueError(f"expected contiguous float32 points of shape ({self.stride_size}, {self.dim})")
+        for o in (label, cluster_id):
+            if not (isinstance(o, np.ndarray) and o.dtype == np.int32 and o.flags.c_contiguous
+                    and o.shape == (self.window_size,)):
+                raise ValueError(f"expected contiguous int32 outputs of shape ({self.window_size},)")
+        _check(self._lib.rtdbs_slide_pipelined(self._h, a.ctypes.data, label.ctypes.data, cluster_id.ctypes.data))
 
     def cluster(self):
         lab = np.empty(self.window_size, np.int32)

@@ -192,6 +192,33 @@ def test_slide_async_device_buffers():
     eng.close()
 
 
+def test_slide_pipelined_host_buffers():
+    """One slide in flight: each call returns the previous slide's result into
+    that call's (pinned) buffers; the last one arrives with sync()."""
+    torch = pytest.importorskip("torch")
+    W, S, n = 8_000, 1_000, 6
+    pts = wl.gaussian_mixture(W + n * S, dim=3, k=8, box=20.0, seed=21)
+    exp = O.stream(pts, W, S, 0.8, 6, O.MODE_FP64, first_slide=1, n_out=n)
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt).pin_memory().numpy()
+    h_in = pin((W + n * S, 3), torch.float32)
+    h_in[:] = pts
+    outs = [(pin(W, torch.int32), pin(W, torch.int32)) for _ in range(n)]
+    with Engine(3, W, S, 0.8, 6) as eng:
+        eng.load_window(h_in[:W])
+        for k in range(n):
+            eng.slide_pipelined(h_in[W + k * S: W + (k + 1) * S], *outs[k])
+            if k:  # the previous slide is complete
+                lab, cid = outs[k - 1]
+                assert np.array_equal(lab, exp[1][k - 1]), k - 1
+                keep = exp[1][k - 1] != 2
+                assert np.array_equal(cid[keep], exp[2][k - 1][keep]), k - 1
+        eng.sync()
+        lab, cid = outs[n - 1]
+        assert np.array_equal(lab, exp[1][n - 1])
+        assert np.array_equal(cid[exp[1][n - 1] != 2], exp[2][n - 1][exp[1][n - 1] != 2])
+        assert np.array_equal(eng.counts(), exp[0][n - 1])
+
+
 def test_cluster_twice_without_slide():
     pts = wl.gaussian_mixture(4_000 + 1_000, dim=3, k=6, box=15.0, seed=15)
     with Engine(3, 4_000, 1_000, 1.0, 5) as eng:
