@@ -179,8 +179,14 @@ struct rtdbs_engine {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double cell_side = 0.0;
-    // rtdbs_slide_pipelined: the end of the last two pipelined slides, and
-    // whether one is still in flight
+    // rtdbs_slide_pipelined: the outputs go to the host on their own stream
+    // (`copy`) while the next slide runs; ev_done marks a slide's end on the
+    // engine's stream, ev_free the end of its output copies, which every
+    // slide's label pass waits for (a wait node in the captured graph);
+    // ev_pipe marks the last two pipelined slides complete, and
+    // pipe_pending says whether one is still in flight
+    cudaStream_t copy = nullptr;
+    cudaEvent_t ev_done = nullptr, ev_free = nullptr;
     cudaEvent_t ev_pipe[2] = {nullptr, nullptr};
     int pipe_next = 0;
     bool pipe_pending = false;
@@ -292,7 +298,9 @@ int check_device_error(rtdbs_engine* e) {
     return RTDBS_OK;
 }
 
-int enqueue_slide(rtdbs_engine* e) {
+// (capturing: the label pass's wait for the last output copies becomes an
+// external-event wait node of the graph)
+int enqueue_slide(rtdbs_engine* e, bool capturing) {
     const int S = e->p.stride, C = e->chunk;
     const int nchunks = (S + C - 1) / C;
     for (int j = 0; j < nchunks; ++j) {
@@ -300,7 +308,14 @@ int enqueue_slide(rtdbs_engine* e) {
         CUDA_TRY(rtdbs::launch_chunk_step(e->v, e->p.precision, j, c, 0, j * C, e->stream, e->side, e->ev_fork,
                                           e->ev_join));
     }
-    CUDA_TRY(rtdbs::launch_cluster(e->v, e->p.precision, 1, e->stream));
+    CUDA_TRY(rtdbs::launch_cluster(e->v, e->p.precision, 1, e->stream, false, e->ev_free,
+                                   capturing ? cudaEventWaitExternal : cudaEventWaitDefault));
+    return RTDBS_OK;
+}
+
+// Orders later label writes (outside a slide graph) after the last output copies.
+int wait_outputs_free(rtdbs_engine* e) {
+    if (e->ev_free) CUDA_TRY(cudaStreamWaitEvent(e->stream, e->ev_free, 0));
     return RTDBS_OK;
 }
 
@@ -309,6 +324,9 @@ int ensure_side(rtdbs_engine* e) {
     if (e->side) return RTDBS_OK;
     CUDA_TRY(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&e->ev_done, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&e->ev_free, cudaEventDisableTiming));
+    CUDA_TRY(cudaStreamCreateWithFlags(&e->copy, cudaStreamNonBlocking));
     CUDA_TRY(cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking));
     return RTDBS_OK;
 }
@@ -316,11 +334,11 @@ int ensure_side(rtdbs_engine* e) {
 int run_slide(rtdbs_engine* e) {
     int rc0 = ensure_side(e);  // before any capture
     if (rc0 != RTDBS_OK) return rc0;
-    if (e->p.flags & RTDBS_FLAG_NO_GRAPH) return enqueue_slide(e);
+    if (e->p.flags & RTDBS_FLAG_NO_GRAPH) return enqueue_slide(e, false);
     if (!e->slide_graph) {
         cudaGraph_t g = nullptr;
         CUDA_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = enqueue_slide(e);
+        int rc = enqueue_slide(e, true);
         cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
         if (rc != RTDBS_OK) {
             if (g) cudaGraphDestroy(g);
@@ -354,6 +372,7 @@ int copy_out(rtdbs_engine* e, int32_t* label, int32_t* cid, int on_device) {
 int fetch_ctl_and_sync(rtdbs_engine* e) {
     CUDA_TRY(cudaMemcpyAsync(e->h_ctl, e->v.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->stream));
     CUDA_TRY(cudaStreamSynchronize(e->stream));
+    if (e->copy) CUDA_TRY(cudaStreamSynchronize(e->copy));
     e->pipe_pending = false;  // everything queued, pipelined slides included, is done
     return check_device_error(e);
 }
@@ -466,6 +485,12 @@ int rtdbs_destroy(rtdbs_engine* e) {
     if (e->dev_block) cudaFree(e->dev_block);
     if (e->h_ctl) cudaFreeHost(e->h_ctl);
     if (e->side) cudaStreamDestroy(e->side);
+    if (e->copy) {
+        cudaStreamSynchronize(e->copy);
+        cudaStreamDestroy(e->copy);
+    }
+    if (e->ev_done) cudaEventDestroy(e->ev_done);
+    if (e->ev_free) cudaEventDestroy(e->ev_free);
     if (e->ev_fork) cudaEventDestroy(e->ev_fork);
     for (auto& ev : e->ev_pipe)
         if (ev) cudaEventDestroy(ev);
@@ -562,13 +587,19 @@ int rtdbs_slide_pipelined(rtdbs_engine* e, const float* new_points, int32_t* lab
         if (!ev) CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     int rc = copy_in(e, new_points, e->p.stride, 0);
     if (rc == RTDBS_OK) rc = run_slide(e);
-    if (rc == RTDBS_OK) rc = copy_out(e, label, cluster_id, 0);
     if (rc != RTDBS_OK) return rc;
-    // the control block follows the slide's outputs, so the previous slide's
-    // error bits are on the host once its event has passed
-    CUDA_TRY(cudaMemcpyAsync(e->h_ctl, e->v.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->stream));
+    // the outputs (and the control block, whose error bits the call that
+    // completes this slide reads) go to the host on the copy stream while
+    // the next slide runs; its label pass waits for ev_free
+    CUDA_TRY(cudaEventRecord(e->ev_done, e->stream));
+    CUDA_TRY(cudaStreamWaitEvent(e->copy, e->ev_done, 0));
+    const size_t bytes = sizeof(int) * e->p.window;
+    if (label) CUDA_TRY(cudaMemcpyAsync(label, e->v.label, bytes, cudaMemcpyDeviceToHost, e->copy));
+    if (cluster_id) CUDA_TRY(cudaMemcpyAsync(cluster_id, e->v.cid, bytes, cudaMemcpyDeviceToHost, e->copy));
+    CUDA_TRY(cudaMemcpyAsync(e->h_ctl, e->v.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->copy));
+    CUDA_TRY(cudaEventRecord(e->ev_free, e->copy));
     const int cur = e->pipe_next;
-    CUDA_TRY(cudaEventRecord(e->ev_pipe[cur], e->stream));
+    CUDA_TRY(cudaEventRecord(e->ev_pipe[cur], e->copy));
     e->pipe_next = cur ^ 1;
     const bool wait_prev = e->pipe_pending;
     e->pipe_pending = true;
@@ -589,6 +620,8 @@ int rtdbs_cluster(rtdbs_engine* e, int32_t* label, int32_t* cluster_id, int on_d
     if (!e->loaded) return fail(RTDBS_ERR_STATE, "rtdbs_load_window must come first");
     DeviceGuard guard(e->device);
     CUDA_TRY(guard.err);
+    const int rc0 = wait_outputs_free(e);
+    if (rc0 != RTDBS_OK) return rc0;
     CUDA_TRY(rtdbs::launch_cluster(e->v, e->p.precision, 0, e->stream, true));
     int rc = copy_out(e, label, cluster_id, on_device);
     if (rc == RTDBS_OK) rc = fetch_ctl_and_sync(e);
@@ -665,8 +698,8 @@ int rtdbs_slide_profiled(rtdbs_engine* e, const float* d_new_points, rtdbs_phase
     const int nev = nchunks * rtdbs::kChunkPhases + 4;
     std::vector<cudaEvent_t> ev(nev, nullptr);
     for (auto& x : ev) CUDA_TRY(cudaEventCreate(&x));
-    int rc = RTDBS_OK;
-    if (d_new_points != e->v.staging) rc = copy_in(e, d_new_points, S, 1);
+    int rc = wait_outputs_free(e);
+    if (rc == RTDBS_OK && d_new_points != e->v.staging) rc = copy_in(e, d_new_points, S, 1);
     int k = 0;
     if (rc == RTDBS_OK) {
         cudaEventRecord(ev[k++], e->stream);

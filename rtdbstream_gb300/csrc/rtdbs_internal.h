@@ -175,7 +175,10 @@ cudaError_t launch_chunk_step(const View& v, int precision, int j, int c, int in
                               cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 // fresh_hints: start the union from fresh hints and forest (no reuse), for a
 // clustering of the window as it stands rather than after a slide.
-cudaError_t launch_cluster(const View& v, int precision, int advance, cudaStream_t s, bool fresh_hints = false);
+// outputs_free: an event the label pass (which rewrites label/cid) waits for
+// first, with wait_flags (cudaEventWaitExternal inside a stream capture).
+cudaError_t launch_cluster(const View& v, int precision, int advance, cudaStream_t s, bool fresh_hints = false,
+                           cudaEvent_t outputs_free = nullptr, unsigned wait_flags = 0);
 cudaError_t launch_counts_by_slot(const View& v, int* nn_by_slot, cudaStream_t s);
 cudaError_t configure_kernels();
 

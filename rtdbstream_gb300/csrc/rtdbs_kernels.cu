@@ -1906,15 +1906,18 @@ cudaError_t launch_chunk_step(const View& v, int precision, int j, int c, int in
     return cudaSuccess;
 }
 
-cudaError_t launch_cluster(const View& v, int precision, int advance, cudaStream_t s, bool fresh_hints) {
+cudaError_t launch_cluster(const View& v, int precision, int advance, cudaStream_t s, bool fresh_hints,
+                           cudaEvent_t outputs_free, unsigned wait_flags) {
     cudaError_t e = cudaSuccess;
     if (fresh_hints) {
         const int sms = g_num_sms > 0 ? g_num_sms : 152;
         k_hints<<<max(1, min(sms * 8, (v.W + 255) / 256)), 256, 0, s>>>(v);
         e = cudaGetLastError();
     }
-    for (int ph = kPhaseUnion; ph <= kPhaseLabel && e == cudaSuccess; ++ph)
-        e = launch_phase(ph, v, precision, 0, 0, 0, 0, advance, s);
+    for (int ph = kPhaseUnion; ph <= kPhaseLabel && e == cudaSuccess; ++ph) {
+        if (ph == kPhaseLabel && outputs_free) e = cudaStreamWaitEvent(s, outputs_free, wait_flags);
+        if (e == cudaSuccess) e = launch_phase(ph, v, precision, 0, 0, 0, 0, advance, s);
+    }
     return e;
 }
 
