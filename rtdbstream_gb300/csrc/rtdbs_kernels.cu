@@ -974,8 +974,10 @@ __device__ __forceinline__ void merge_body(const View& v, int j, int c, int init
     unsigned long long* dkey = v.skey[dst];
     float4* dpt = v.spt[dst];
     int* dcnt = v.scnt[dst];
-    const int* oprev = v.sprev[src];
-    int* dprev = v.sprev[dst];
+    // previous roots are only read by this slide's reuse (a slide without
+    // reuse leaves them to the flatten, which writes them afresh)
+    const int* oprev = reuse ? v.sprev[src] : nullptr;
+    int* dprev = reuse ? v.sprev[dst] : nullptr;
 
     // tile bounds among the new / expired words: warps 0, 1, 2 search at once
     {
@@ -1488,6 +1490,9 @@ __device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx, Str
     const unsigned gen = gen_of_build(b);
     const int* sw = reinterpret_cast<const int*>(v.spt[cur]) + 3;  // .w = slot
     int* nbuf = sm.nbuf[wib];
+    // the roots by position for the next slide's reuse: not while reuse
+    // stays off for it (k_border counts reuse_skip down after this pass)
+    const bool keep_roots = v.ctl->reuse_skip <= 1;
     Tally tally;
     // Roots first (no barrier); the positions whose lists are rebuilt go to
     // the block's queue, which its warps share once the block has been
@@ -1503,10 +1508,10 @@ __device__ __forceinline__ void flatten_body(const View& v, int bx, int nbx, Str
             if (scnt[i] >= v.min_pts) {
                 const int root = uf_find(v.parent, v.sroot[i]);
                 v.rslot[slot] = root;
-                v.sprev[cur][i] = root;  // the next slide's reuse reads it by position
+                if (keep_roots) v.sprev[cur][i] = root;  // the next slide's reuse reads it by position
             } else {
                 v.rslot[slot] = -1;
-                v.sprev[cur][i] = -1;
+                if (keep_roots) v.sprev[cur][i] = -1;
                 need = v.ntrack[slot] != 1;
             }
         }
