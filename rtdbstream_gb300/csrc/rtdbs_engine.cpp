@@ -175,6 +175,7 @@ struct rtdbs_engine {
     bool geometry_ready = false;
     bool loaded = false;
     cudaGraphExec_t slide_graph = nullptr;
+    cudaGraphExec_t pipe_graph = nullptr;  // the slide of rtdbs_slide_pipelined
     // side stream for the decrement pass beside the sort (made on the first slide)
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -298,9 +299,9 @@ int check_device_error(rtdbs_engine* e) {
     return RTDBS_OK;
 }
 
-// (capturing: the label pass's wait for the last output copies becomes an
-// external-event wait node of the graph)
-int enqueue_slide(rtdbs_engine* e, bool capturing) {
+// (pipelined: the label pass first waits for the last output copies; while
+// capturing, that wait becomes an external-event wait node of the graph)
+int enqueue_slide(rtdbs_engine* e, bool capturing, bool pipelined) {
     const int S = e->p.stride, C = e->chunk;
     const int nchunks = (S + C - 1) / C;
     for (int j = 0; j < nchunks; ++j) {
@@ -308,7 +309,7 @@ int enqueue_slide(rtdbs_engine* e, bool capturing) {
         CUDA_TRY(rtdbs::launch_chunk_step(e->v, e->p.precision, j, c, 0, j * C, e->stream, e->side, e->ev_fork,
                                           e->ev_join));
     }
-    CUDA_TRY(rtdbs::launch_cluster(e->v, e->p.precision, 1, e->stream, false, e->ev_free,
+    CUDA_TRY(rtdbs::launch_cluster(e->v, e->p.precision, 1, e->stream, false, pipelined ? e->ev_free : nullptr,
                                    capturing ? cudaEventWaitExternal : cudaEventWaitDefault));
     return RTDBS_OK;
 }
@@ -331,25 +332,35 @@ int ensure_side(rtdbs_engine* e) {
     return RTDBS_OK;
 }
 
-int run_slide(rtdbs_engine* e) {
+// One slide.  pipelined: the slide of rtdbs_slide_pipelined, whose label pass
+// waits inside the graph for the previous slide's output copies (a graph of
+// its own: the wait node costs small windows tens of microseconds per
+// slide); any other slide waits for those copies, if one may still run,
+// before it starts.
+int run_slide(rtdbs_engine* e, bool pipelined = false) {
     int rc0 = ensure_side(e);  // before any capture
     if (rc0 != RTDBS_OK) return rc0;
-    if (e->p.flags & RTDBS_FLAG_NO_GRAPH) return enqueue_slide(e, false);
-    if (!e->slide_graph) {
+    if (!pipelined && e->pipe_pending) {
+        rc0 = wait_outputs_free(e);
+        if (rc0 != RTDBS_OK) return rc0;
+    }
+    if (e->p.flags & RTDBS_FLAG_NO_GRAPH) return enqueue_slide(e, false, pipelined);
+    cudaGraphExec_t& exec = pipelined ? e->pipe_graph : e->slide_graph;
+    if (!exec) {
         cudaGraph_t g = nullptr;
         CUDA_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = enqueue_slide(e, true);
+        int rc = enqueue_slide(e, true, pipelined);
         cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
         if (rc != RTDBS_OK) {
             if (g) cudaGraphDestroy(g);
             return rc;
         }
         CUDA_TRY(ce);
-        cudaError_t ie = cudaGraphInstantiate(&e->slide_graph, g, 0);
+        cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
         cudaGraphDestroy(g);
         CUDA_TRY(ie);
     }
-    CUDA_TRY(cudaGraphLaunch(e->slide_graph, e->stream));
+    CUDA_TRY(cudaGraphLaunch(exec, e->stream));
     return RTDBS_OK;
 }
 
@@ -456,7 +467,7 @@ int rtdbs_create(const rtdbs_params* params, void* cuda_stream, rtdbs_engine** o
     View& v = e->v;
     v.dim = p.dim;
     v.cell_mult = p.cell_mult > 0 ? p.cell_mult : 1;
-    v.grab = p.work_grab > 0 ? p.work_grab : rtdbs::kBatch;
+    v.grab = p.work_grab;  // 0: by launch kind and window size (work_grab in the kernels)
     v.qlanes = p.query_lanes > 0 ? p.query_lanes : (v.cell_mult == 1 ? rtdbs::kQueryLanes : 32);
     v.W = p.window;
     v.S = p.stride;
@@ -482,6 +493,7 @@ int rtdbs_destroy(rtdbs_engine* e) {
     DeviceGuard guard(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
     if (e->slide_graph) cudaGraphExecDestroy(e->slide_graph);
+    if (e->pipe_graph) cudaGraphExecDestroy(e->pipe_graph);
     if (e->dev_block) cudaFree(e->dev_block);
     if (e->h_ctl) cudaFreeHost(e->h_ctl);
     if (e->side) cudaStreamDestroy(e->side);
@@ -535,6 +547,10 @@ int rtdbs_load_window(rtdbs_engine* e, const float* points, int points_on_device
         cudaGraphExecDestroy(e->slide_graph);
         e->slide_graph = nullptr;
     }
+    if (e->pipe_graph) {
+        cudaGraphExecDestroy(e->pipe_graph);
+        e->pipe_graph = nullptr;
+    }
     CUDA_TRY(cudaMemsetAsync(e->v.ctl, 0, sizeof(Ctl), e->stream));
     CUDA_TRY(cudaMemsetAsync(e->v.table[0], 0, sizeof(ulonglong2) * ((size_t)e->v.pmask + 1), e->stream));
     CUDA_TRY(cudaMemsetAsync(e->v.table[1], 0, sizeof(ulonglong2) * ((size_t)e->v.pmask + 1), e->stream));
@@ -586,7 +602,7 @@ int rtdbs_slide_pipelined(rtdbs_engine* e, const float* new_points, int32_t* lab
     for (auto& ev : e->ev_pipe)
         if (!ev) CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     int rc = copy_in(e, new_points, e->p.stride, 0);
-    if (rc == RTDBS_OK) rc = run_slide(e);
+    if (rc == RTDBS_OK) rc = run_slide(e, true);
     if (rc != RTDBS_OK) return rc;
     // the outputs (and the control block, whose error bits the call that
     // completes this slide reads) go to the host on the copy stream while

@@ -1329,8 +1329,17 @@ struct ClusterSmem {
     int rstart[kClusterThreads / 32][kMaxRows], rpre[kClusterThreads / 32][kMaxRows + 1];
 };
 
+// Work items a warp takes at a time: the stream's setting, or by default 8
+// in a pool launch (many streams share the GPU) and for a single stream 8 on
+// large windows, fewer on small ones (a 10k-point window has a few hundred to
+// a few thousand items: 8 per grab would leave them to a few dozen warps).
+__device__ __forceinline__ int work_grab(const View& v, bool pooled) {
+    if (v.grab > 0) return v.grab;
+    return pooled ? kBatch : max(1, min(kBatch, v.W >> 14));
+}
+
 template <int MODE, int DK>
-__device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
+__device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm, int grab) {
     constexpr int DIM = DK & 3, K = (DK >> 2) + 1;  // dimension, cells per Eps
     float4(&home_pt)[kClusterThreads / 32][32] = sm.home_pt;
     int(&rstart)[kClusterThreads / 32][kMaxRows] = sm.rstart;
@@ -1354,17 +1363,17 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
     volatile int* hint = v.sroot;
     Tally tally;
     int err = 0;
-    // Warps take batches of v.grab consecutive work items (neighbouring
+    // Warps take batches of `grab` consecutive work items (neighbouring
     // cells: candidate loads reuse L1) from a counter, so uneven items do not
     // leave warps idle at the end.
     int it1 = 0;
     for (int itx = nitems;;) {
         if (itx >= it1) {
             int got = 0;
-            if (lane == 0) got = atomicAdd(&v.ctl->union_next, v.grab);
+            if (lane == 0) got = atomicAdd(&v.ctl->union_next, grab);
             itx = __shfl_sync(kFull, got, 0);
             if (itx >= nitems) break;
-            it1 = min(itx + v.grab, nitems);
+            it1 = min(itx + grab, nitems);
         }
         const int2 item = v.items[itx++];
         const int start = item.x, len = item.y;
@@ -1436,7 +1445,7 @@ __device__ __forceinline__ void union_body(const View& v, ClusterSmem& sm) {
 template <int MODE, int DK>
 __global__ void __launch_bounds__(kClusterThreads, 8) k_union(View v) {
     __shared__ ClusterSmem sm;
-    union_body<MODE, DK>(v, sm);
+    union_body<MODE, DK>(v, sm, work_grab(v, false));
 }
 
 // The neighbour list of the non-core point at sorted position `at`, from one
@@ -1545,7 +1554,7 @@ __global__ void __launch_bounds__(256, 6) k_flatten(View v) {
 // Labels and ids by slot: core -> 0 and its root; non-core -> 1 and the
 // minimum root over adjacent cores, or 2 and its own slot.
 template <int MODE, int DK>
-__device__ __forceinline__ void label_body(const View& v, int advance, int bx, ClusterSmem& sm) {
+__device__ __forceinline__ void label_body(const View& v, int advance, int bx, ClusterSmem& sm, int grab) {
     constexpr int DIM = DK & 3, K = (DK >> 2) + 1;  // dimension, cells per Eps
     int(&rstart)[kClusterThreads / 32][kMaxRows] = sm.rstart;
     int(&rpre)[kClusterThreads / 32][kMaxRows + 1] = sm.rpre;
@@ -1565,10 +1574,10 @@ __device__ __forceinline__ void label_body(const View& v, int advance, int bx, C
     for (int itx = nitems;;) {
         if (itx >= it1) {
             int got = 0;
-            if (lane == 0) got = atomicAdd(&v.ctl->label_next, v.grab);
+            if (lane == 0) got = atomicAdd(&v.ctl->label_next, grab);
             itx = __shfl_sync(kFull, got, 0);
             if (itx >= nitems) break;
-            it1 = min(itx + v.grab, nitems);
+            it1 = min(itx + grab, nitems);
         }
         const int2 item = v.items[itx++];
         const int start = item.x, len = item.y;
@@ -1637,7 +1646,7 @@ __device__ __forceinline__ void label_body(const View& v, int advance, int bx, C
 template <int MODE, int DK>
 __global__ void __launch_bounds__(kClusterThreads, 6) k_label(View v, int advance) {
     __shared__ ClusterSmem sm;
-    label_body<MODE, DK>(v, advance, blockIdx.x, sm);
+    label_body<MODE, DK>(v, advance, blockIdx.x, sm, work_grab(v, false));
 }
 
 // Outputs by slot from the roots and the lists: core -> 0 and its root; a
@@ -1771,7 +1780,7 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
         incr_body<MODE, DK>(sv, it.j, it.c, 0, bx, sm);
     } else if constexpr (PHASE == kBatchUnion) {
         __shared__ ClusterSmem sm;
-        union_body<MODE, DK>(sv, sm);
+        union_body<MODE, DK>(sv, sm, work_grab(sv, true));
     } else if constexpr (PHASE == kBatchFlatten) {
         __shared__ StreamSmem sm;
         flatten_body<MODE, DK>(sv, bx, nbx, sm);
@@ -1780,7 +1789,7 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
         if (sv.list_cap >= 0)
             border_body(sv, 1, bx, nbx);
         else
-            label_body<MODE, DK>(sv, 1, bx, sm);
+            label_body<MODE, DK>(sv, 1, bx, sm, work_grab(sv, true));
     }
 }
 
@@ -1870,8 +1879,9 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
             [[fallthrough]];
         case kPhaseUnion: {
             const int sms = g_num_sms > 0 ? g_num_sms : 152;
-            const int per_block = kClusterThreads / 32;
-            const int need = (v.max_items + per_block - 1) / per_block;  // one warp per item at most
+            // queue-fed blocks: one warp per ~12 window points (a few items
+            // each on sparse windows), all the SMs hold on large ones
+            const int need = (v.W + 95) / 96;
             const int blocks = max(1, min(sms * 6, need));
             if (phase == kPhaseUnion)
                 RTDBS_DISPATCH(precision, dk_of(v), k_union, max(1, min(sms * 8, need)), kClusterThreads, s, v);
@@ -1881,7 +1891,7 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
         }
         case kPhaseFlatten: {
             const int sms = g_num_sms > 0 ? g_num_sms : 152;
-            RTDBS_DISPATCH(precision, dk_of(v), k_flatten, sms * 16, 256, s, v);
+            RTDBS_DISPATCH(precision, dk_of(v), k_flatten, max(1, min(sms * 16, (v.W + 255) / 256)), 256, s, v);
             break;
         }
         default:

@@ -179,7 +179,7 @@ extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int
     std::memset(&v, 0, sizeof(v));
     v.dim = dim;
     v.cell_mult = 1;
-    v.grab = rtdbs::kBatch;
+    v.grab = 0;  // the default work split for the window's size
     v.qlanes = rtdbs::kQueryLanes;
     v.W = n;
     v.S = n;
