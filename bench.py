@@ -309,14 +309,16 @@ def algorithmic_bytes(phase: str, W: int, S: int, dim: int, cells: int, items: i
         "ingest": c * (4 * dim + 16 + 8 + 16 + 8 + 8 + 8 + 16),
         "sort": 2 * c * 16,
         "decrement": c * (8 + 16),
-        "merge": W * (28 + 28 + 4) + c * (8 + 16),
+        # (key, point, count) read and written, root hint written, the previous
+        # root carried (read and written) while forest reuse is on
+        "merge": W * (28 + 28 + 4 + 8) + c * (8 + 16),
         "build": W * 8 + cells * 32 + items * 8,
         "increment": c * (8 + 16) + c * 4,
         "union": W * (16 + 4 + 4 + 4),
-        # scnt, slot, root hint, parent read; root by slot written
-        "flatten": W * (4 + 4 + 4 + 4 + 4),
-        # border pass: root by slot read; label, cid, parent written
-        "label": W * (4 + 4 + 4 + 4),
+        # scnt, slot, root hint, parent read; root by slot and by position written
+        "flatten": W * (4 + 4 + 4 + 4 + 4 + 4),
+        # border pass: root by slot read; label, cid, parent, damage mark written
+        "label": W * (4 + 4 + 4 + 4 + 4),
     }[phase]
 
 
