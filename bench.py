@@ -728,6 +728,9 @@ def run_batched(args, dev, stream, flush, world=1, rank=0, n_streams=256, rounds
                                           query_lanes=c["query_lanes"]))
         pool.load_window(sid, d[:st.window])
         ids.append(sid)
+    # the mean neighbour count (self included) each stream's Eps gives, from
+    # the engine's exact counts of its first window
+    mean_nn = np.array([float(pool.counts(sid).mean()) for sid in ids])
     for k in range(args.warmup):
         pool.slide(ids, packed[k])
     pool.sync()
@@ -810,6 +813,11 @@ def run_batched(args, dev, stream, flush, world=1, rank=0, n_streams=256, rounds
                                         "config": "1 cell per Eps, 8 items per grab, 16 lanes per count query"},
         "launches_per_round": stats["launches_per_round"], "graph_replays": stats["graph_replays"],
         "streams_exact_vs_fp64_oracle": f"{len(all_streams) - int(round(n_diff))}/{len(all_streams)}",
+        "mean_neighbours_measured": {"min": round(float(mean_nn.min()), 1),
+                                     "median": round(float(np.median(mean_nn)), 1),
+                                     "max": round(float(mean_nn.max()), 1),
+                                     "streams_in_10_30": f"{int(((mean_nn >= 10) & (mean_nn <= 30)).sum())}/{len(mean_nn)}",
+                                     "source": "exact counts of each stream's first window (rank 0's streams)"},
         "streams_per_rank": n_streams, "sharding": f"{world} rank(s), streams partitioned by W, no collective",
         "phase_ms": prof,
         "autotune": {"buckets": len(tuner.cache), "tuned_now": tuner.tuned, "tune_s": round(tuner.tune_seconds, 2),
