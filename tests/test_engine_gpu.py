@@ -219,6 +219,48 @@ def test_slide_pipelined_host_buffers():
         assert np.array_equal(eng.counts(), exp[0][n - 1])
 
 
+def test_slide_pipelined_mixed_with_other_calls():
+    """Pipelined slides interleaved with device-buffer slides, counts and a
+    re-cluster: every result matches the oracle (the pipelined slide's
+    output copies finish before any later call rewrites the labels)."""
+    torch = pytest.importorskip("torch")
+    W, S, n = 6_000, 1_500, 7
+    pts = wl.gaussian_mixture(W + n * S, dim=2, k=6, box=25.0, seed=23)
+    exp = O.stream(pts, W, S, 0.6, 5, O.MODE_FP64, first_slide=1, n_out=n)
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt).pin_memory().numpy()
+    outs = [(pin(W, torch.int32), pin(W, torch.int32)) for _ in range(n)]
+    dev = torch.from_numpy(pts).cuda()
+    d_lab = torch.empty(W, dtype=torch.int32, device="cuda")
+    d_cid = torch.empty(W, dtype=torch.int32, device="cuda")
+
+    def same(lab, cid, k):
+        keep = exp[1][k] != 2
+        return np.array_equal(lab, exp[1][k]) and np.array_equal(cid[keep], exp[2][k][keep])
+
+    with Engine(2, W, S, 0.6, 5) as eng:
+        eng.load_window(pts[:W])
+        new = lambda k: np.ascontiguousarray(pts[W + k * S: W + (k + 1) * S])
+        eng.slide_pipelined(new(0), *outs[0])
+        eng.slide_pipelined(new(1), *outs[1])
+        assert same(*outs[0], 0)
+        # a device-buffer slide while slide 1's copies may still run
+        eng.slide_async(dev[W + 2 * S: W + 3 * S].contiguous(), d_lab, d_cid)
+        eng.sync()
+        assert same(*outs[1], 1)
+        assert same(d_lab.cpu().numpy(), d_cid.cpu().numpy(), 2)
+        eng.slide_pipelined(new(3), *outs[3])
+        assert np.array_equal(eng.counts(), exp[0][3])  # synchronising: slide 3 is complete
+        assert same(*outs[3], 3)
+        lab, cid = eng.cluster()  # the window as it stands: slide 3's clustering again
+        assert same(lab, cid, 3)
+        eng.slide_pipelined(new(4), *outs[4])
+        lab, cid = eng.slide(new(5))  # synchronous slide after a pipelined one
+        assert same(*outs[4], 4) and same(lab, cid, 5)
+        eng.slide_pipelined(new(6), *outs[6])
+        eng.sync()
+        assert same(*outs[6], 6)
+
+
 def test_cluster_twice_without_slide():
     pts = wl.gaussian_mixture(4_000 + 1_000, dim=3, k=6, box=15.0, seed=15)
     with Engine(3, 4_000, 1_000, 1.0, 5) as eng:
