@@ -226,7 +226,11 @@ size_t plan_layout(rtdbs_engine* e, std::vector<Part>& parts) {
     }
     v.pbits = pbits;
     v.pmask = (unsigned)(P - 1);
-    v.max_items = W + W / 32 + 64;
+    // work items: cell runs cut at 32 points, at 8 below 65,536 points (a small
+    // window is a few waves of items at most, so its densest cells must not
+    // be one warp's long chain)
+    v.item_pts = W < 65536 ? 8 : 32;
+    v.max_items = W + W / v.item_pts + 64;
     // Neighbour lists of non-core points (MinPts - 2 entries each) replace the
     // label pass's grid scan up to kListCap entries; above that the scan stays.
     const int mp = e->p.min_pts;

@@ -108,6 +108,9 @@ struct View {
     int key_bits;
     int sort_passes;
     int max_items;
+    int item_pts;               // most points of a work item slid alone (8 or 32; 0 = 32; pool
+                                // launches take 32): small windows take short items, so
+                                // dense cells spread over more warps
     int precision;              // RTDBS_PREC_* (batched launches dispatch on it)
     int list_cap;               // entries per neighbour list; -1: no lists (the
                                 // label pass then scans the grid)

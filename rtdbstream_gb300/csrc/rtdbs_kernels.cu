@@ -1113,7 +1113,8 @@ struct BuildSmem {
     int bcells;
 };
 
-__device__ __forceinline__ void build_body(const View& v, int bx, BuildSmem& sm) {
+// (pooled: a pool launch, whose many streams fill the GPU: 32-point items)
+__device__ __forceinline__ void build_body(const View& v, int bx, BuildSmem& sm, bool pooled) {
     int* wcount = sm.wcount;
     int* wbase = sm.wbase;
     int& bcells = sm.bcells;
@@ -1148,7 +1149,8 @@ __device__ __forceinline__ void build_body(const View& v, int bx, BuildSmem& sm)
     }
     if (last && !(firsts & ((2u << lane) - 1u)) && !table_set(T, v.pmask, v.pbits, tag, 1, i + 1))
         err |= kErrHashFull;
-    const unsigned starts = __ballot_sync(kFull, valid && (first || lane == 0));
+    const int ip = (!pooled && v.item_pts > 0) ? v.item_pts : 32;
+    const unsigned starts = __ballot_sync(kFull, valid && (first || (lane & (ip - 1)) == 0));
     const int nfirst = __popc(__ballot_sync(kFull, first));
     if (threadIdx.x == 0) bcells = 0;
     if (lane == 0) wcount[wib] = __popc(starts);
@@ -1165,7 +1167,7 @@ __device__ __forceinline__ void build_body(const View& v, int bx, BuildSmem& sm)
     }
     __syncthreads();
     if (threadIdx.x == 0 && bcells) atomicAdd(&v.ctl->ncells, bcells);
-    if (valid && (first || lane == 0)) {
+    if (valid && (first || (lane & (ip - 1)) == 0)) {
         const int rank = __popc(starts & lanemask_lt(lane));
         const unsigned above = starts & ~((2u << lane) - 1u);
         const int next = above ? gw * 32 + __ffs(above) - 1 : gw * 32 + 32;
@@ -1181,7 +1183,7 @@ __device__ __forceinline__ void build_body(const View& v, int bx, BuildSmem& sm)
 
 __global__ void __launch_bounds__(kBuildThreads) k_build(View v) {
     __shared__ BuildSmem sm;
-    build_body(v, blockIdx.x, sm);
+    build_body(v, blockIdx.x, sm, false);
 }
 
 // Full count of each new point and +1 on every older neighbour (new grid).
@@ -1774,7 +1776,7 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
         merge_body(sv, it.j, it.c, 0, bx, nbx, sm);
     } else if constexpr (PHASE == kBatchBuild) {
         __shared__ BuildSmem sm;
-        build_body(sv, bx, sm);
+        build_body(sv, bx, sm, true);
     } else if constexpr (PHASE == kBatchIncrement) {
         __shared__ StreamSmem sm;
         incr_body<MODE, DK>(sv, it.j, it.c, 0, bx, sm);
