@@ -702,9 +702,14 @@ int rtdbs_get_stats(rtdbs_engine* e, rtdbs_stats* s) {
     s->device_bytes = (int64_t)e->dev_bytes;
     const int nchunks = (e->p.stride + e->chunk - 1) / e->chunk;
     s->chunks_per_slide = nchunks;
-    // per chunk 7 kernels (the sort phase is 2); then union, flatten and
-    // label (or border)
-    s->launches_per_slide = nchunks * (rtdbs::kChunkPhases + 1) + 3;
+    // per chunk 6 kernels, 7 when the sort phase needs a run merge (a chunk
+    // of more than one sort run); then union, flatten and label (or border)
+    int launches = 3;
+    for (int j = 0; j < nchunks; ++j) {
+        const int c = std::min(e->chunk, e->p.stride - j * e->chunk);
+        launches += rtdbs::kChunkPhases + (c > rtdbs::kSortRun ? 1 : 0);
+    }
+    s->launches_per_slide = launches;
     return RTDBS_OK;
 }
 

@@ -650,16 +650,35 @@ struct SortSmem {
     unsigned wsum[32];
 };
 
-__device__ __forceinline__ void sort_body(const View& v, int c, int init, int bx, int by, SortSmem& sm) {
+// single: the chunk is one run (c <= kSortRun), so the sorted run is the
+// final list: it goes straight to nword / xword (and presorted expired words
+// are gathered here), and no run merge follows.
+__device__ __forceinline__ void sort_body(const View& v, int j, int c, int init, int bx, int by, SortSmem& sm,
+                                          bool single) {
     unsigned long long* buf = sm.buf;
     unsigned* whist = sm.whist;
     unsigned* wsum = sm.wsum;
     const int which = by;
-    if (which == 1 && (init || expired_presorted(v, init))) return;
+    if (which == 1 && init) return;
+    if (which == 1 && expired_presorted(v, init)) {
+        if (single) {  // the run merge's gather of the kept order
+            const int i = threadIdx.x;
+            if (i >= c) return;
+            const int k = v.sorder[chunk_base_slot(v, j, 0) + i];
+            if (k < 0 || k >= c) {
+                atomicOr(&v.ctl->err, kErrChunk);
+                v.xword[i] = ~0ull;
+                return;
+            }
+            v.xword[i] = v.xsort[k];
+        }
+        return;
+    }
     const int r0 = bx * kSortRun;
     const int len = min(kSortRun, c - r0);
     if (len <= 0) return;
     unsigned long long* run = (which ? v.xsort : v.nsort) + r0;  // sorted in place
+    unsigned long long* dst = single ? (which ? v.xword : v.nword) : run;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const unsigned lt = lanemask_lt(lane);
     unsigned long long it = tid < len ? run[tid] : ~0ull;
@@ -696,12 +715,12 @@ __device__ __forceinline__ void sort_body(const View& v, int c, int init, int bx
         __syncthreads();
         it = buf[tid];
     }
-    if (tid < len) run[tid] = it;
+    if (tid < len) dst[tid] = it;
 }
 
-__global__ void __launch_bounds__(kSortRun) k_sort(View v, int c, int init) {
+__global__ void __launch_bounds__(kSortRun) k_sort(View v, int j, int c, int init, int single) {
     __shared__ SortSmem sm;
-    sort_body(v, c, init, blockIdx.x, blockIdx.y, sm);
+    sort_body(v, j, c, init, blockIdx.x, blockIdx.y, sm, single != 0);
 }
 
 // Merges the sorted runs of kSortRun words into one sorted list: a word's
@@ -1763,7 +1782,7 @@ __global__ void __launch_bounds__(PhaseShape<PHASE>::threads, PhaseShape<PHASE>:
     } else if constexpr (PHASE == kBatchSort) {
         __shared__ SortSmem sm;
         const int nruns = (it.c + kSortRun - 1) / kSortRun;
-        sort_body(sv, it.c, 0, bx % nruns, bx / nruns, sm);
+        sort_body(sv, it.j, it.c, 0, bx % nruns, bx / nruns, sm, false);
     } else if constexpr (PHASE == kBatchRunmerge) {
         extern __shared__ unsigned long long words[];
         const int nruns = (it.c + kSortRun - 1) / kSortRun;
@@ -1854,12 +1873,15 @@ cudaError_t launch_phase(int phase, const View& v, int precision, int j, int c, 
         case kPhaseIngest:
             k_ingest<<<(c + 255) / 256, 256, 0, s>>>(v, j, c, init, stg_off);
             break;
-        case kPhaseSort:
-            k_sort<<<dim3((c + kSortRun - 1) / kSortRun, init ? 1 : 2), kSortRun, 0, s>>>(v, c, init);
+        case kPhaseSort: {
+            const int single = c <= kSortRun;  // one run: sorted straight into place, no run merge
+            k_sort<<<dim3((c + kSortRun - 1) / kSortRun, init ? 1 : 2), kSortRun, 0, s>>>(v, j, c, init, single);
+            if (single) break;
             ensure_runmerge_smem();
             k_runmerge<<<dim3((c + kSortRun - 1) / kSortRun, init ? 1 : 2), kSortRun,
                          sizeof(unsigned long long) * c, s>>>(v, j, c, init);
             break;
+        }
         case kPhaseDecrement:
             if (!init) RTDBS_DISPATCH(precision, dk_of(v), k_decr, warp_blocks, 256, s, v, j, c);
             break;
