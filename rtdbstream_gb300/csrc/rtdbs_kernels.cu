@@ -200,18 +200,26 @@ __device__ __forceinline__ void sqdist32x2(const float4& a, const float4& b0, co
 
 // ---------------------------------------------------------------- cell table
 
+// Home slot of a cell key: the key folded to 32 bits, then Fibonacci
+// hashing (pbits <= 31); keys below 2^32 fold to themselves, so the stencil
+// lookups of small grids hash in 32-bit arithmetic (table_home32).
+__device__ __forceinline__ unsigned table_home32(unsigned key, int pbits) {
+    return (key * 0x9E3779B1u) >> (32 - pbits);
+}
+
 __device__ __forceinline__ unsigned table_home(unsigned long long key, int pbits) {
-    return (unsigned)((key * 0x9E3779B97F4A7C15ull) >> (64 - pbits));
+    return table_home32((unsigned)key ^ (unsigned)(key >> 32), pbits);
 }
 
 __device__ __forceinline__ unsigned long long tag_of(unsigned long long key, unsigned gen) {
     return ((unsigned long long)gen << kKeyBitsMax) | key;
 }
 
-// [start, end) of a cell, (0, 0) if the cell is empty in this generation.
-__device__ __forceinline__ int2 table_find(const ulonglong2* T, unsigned pmask, int pbits,
-                                           unsigned long long tag) {
-    unsigned s = table_home(tag & kKeyMask, pbits);
+// [start, end) of a cell, (0, 0) if the cell is empty in this generation;
+// `home` is the key's home slot.
+__device__ __forceinline__ int2 table_find_at(const ulonglong2* T, unsigned pmask, unsigned home,
+                                              unsigned long long tag) {
+    unsigned s = home;
     const unsigned long long gen = tag >> kKeyBitsMax;
     for (unsigned i = 0; i <= pmask; ++i) {
         const ulonglong2 e = T[s];
@@ -220,6 +228,11 @@ __device__ __forceinline__ int2 table_find(const ulonglong2* T, unsigned pmask, 
         s = (s + 1) & pmask;
     }
     return make_int2(0, 0);
+}
+
+__device__ __forceinline__ int2 table_find(const ulonglong2* T, unsigned pmask, int pbits,
+                                           unsigned long long tag) {
+    return table_find_at(T, pmask, table_home(tag & kKeyMask, pbits), tag);
 }
 
 // Claims (or finds) the slot of `tag` and stores one half of its range:
@@ -286,10 +299,46 @@ __device__ __forceinline__ void row_ranges(const View& v, const ulonglong2* T, u
     constexpr int kSlots = kW * St::kRows;           // cell slots, kept row by kept row
     constexpr int kPer = (kSlots + G - 1) / G;       // cells per lane
     static_assert(kPer <= 4 && St::kRows <= G, "stencil too large for the lane group");
+    int2 rg[kPer];
+    if (v.key_bits <= 31) {
+        // keys, cell coordinates and extents fit 32 bits: the lookups in
+        // 32-bit arithmetic (coordinates wrap below zero, so one unsigned
+        // comparison bounds each axis)
+        const unsigned k32 = (unsigned)key;
+        const int s0 = v.shift[0], s1 = v.shift[1];
+        const unsigned c2 = k32 & ((1u << s1) - 1u);
+        const unsigned c1 = (k32 >> s1) & ((1u << (s0 - s1)) - 1u);
+        const unsigned c0 = k32 >> s0;
+        const unsigned e0 = (unsigned)v.ext[0], e1 = (unsigned)v.ext[1], e2 = (unsigned)v.ext[2];
+        const unsigned long long gtag = (unsigned long long)gen << kKeyBitsMax;
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            rg[k] = make_int2(0, 0);
+            const int cs = lane + k * G;
+            const int row = St::kFirst + cs / kW, d_last = cs % kW - K;
+            const bool skip = HALF && cs < kW && d_last < 0;
+            if (cs < kSlots && !skip) {
+                unsigned q0 = c0, q1 = c1, q2 = c2;
+                if (DIM == 1) {
+                    q0 += (unsigned)d_last;
+                } else if (DIM == 2) {
+                    q0 += (unsigned)(row - K);
+                    q1 += (unsigned)d_last;
+                } else {
+                    q0 += (unsigned)(row / kW - K);
+                    q1 += (unsigned)(row % kW - K);
+                    q2 += (unsigned)d_last;
+                }
+                if (q0 < e0 && q1 < e1 && q2 < e2) {
+                    const unsigned nk = (q0 << s0) | (q1 << s1) | q2;
+                    rg[k] = table_find_at(T, v.pmask, table_home32(nk, v.pbits), gtag | nk);
+                }
+            }
+        }
+    } else {
     const long long c2 = (long long)(key & ((1ull << v.shift[1]) - 1ull));
     const long long c1 = (long long)((key >> v.shift[1]) & ((1ull << (v.shift[0] - v.shift[1])) - 1ull));
     const long long c0 = (long long)(key >> v.shift[0]);
-    int2 rg[kPer];
 #pragma unroll
     for (int k = 0; k < kPer; ++k) {
         rg[k] = make_int2(0, 0);
@@ -315,6 +364,7 @@ __device__ __forceinline__ void row_ranges(const View& v, const ulonglong2* T, u
                 rg[k] = table_find(T, v.pmask, v.pbits, tag_of(nk, gen));
             }
         }
+    }
     }
     int s = INT_MAX, e = INT_MIN;
 #pragma unroll
