@@ -163,6 +163,7 @@ class MixStream:
     min_pts: int
     seed: int
     box: float
+    target: float = 0.0  # mean neighbour count the Eps was chosen for (0: not recorded)
 
 
 def _divisor_near(W: int, target: int) -> int:
@@ -176,12 +177,15 @@ def _divisor_near(W: int, target: int) -> int:
     return best
 
 
-def mixed_streams(n: int = 256, seed: int = 3, w_lo: int = 1_000, w_hi: int = 200_000) -> list:
+def mixed_streams(n: int = 256, seed: int = 3, w_lo: int = 1_000, w_hi: int = 200_000,
+                  calibrate: bool = False) -> list:
     """Uneven independent streams: dim 2 or 3 (50/50), W log-uniform in
     [w_lo, w_hi], S a divisor of W near U[1%, 10%] of W, Gaussian-mixture data
     (20 Gaussians, sigma 1, 10% uniform noise) in a box scaled so densities
-    differ per stream, Eps for a mean neighbour count drawn from U[10, 30]
-    (see mix_eps), MinPts U[4, 16]."""
+    differ per stream, Eps for a mean neighbour count drawn from U[10, 30],
+    MinPts U[4, 16].  Eps starts from the density estimate of mix_eps; with
+    `calibrate` it is then fitted to each stream's first window
+    (calibrate_eps), as the benchmarks do."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n):
@@ -192,8 +196,8 @@ def mixed_streams(n: int = 256, seed: int = 3, w_lo: int = 1_000, w_hi: int = 20
         box = float(rng.uniform(40.0, 160.0))
         target = float(rng.uniform(10.0, 30.0))
         eps = mix_eps(W, dim, box, target)
-        out.append(MixStream(dim, W, S, eps, int(rng.integers(4, 17)), 1000 + i, box))
-    return out
+        out.append(MixStream(dim, W, S, eps, int(rng.integers(4, 17)), 1000 + i, box, target))
+    return [calibrate_eps(s) for s in out] if calibrate else out
 
 
 def mix_eps(W: int, dim: int, box: float, target: float, k: int = 20, sigma: float = 1.0) -> float:
@@ -206,6 +210,41 @@ def mix_eps(W: int, dim: int, box: float, target: float, k: int = 20, sigma: flo
     if dim == 2:
         return float(np.sqrt(vol / np.pi))
     return float((vol * 3.0 / (4.0 * np.pi)) ** (1.0 / 3.0))
+
+
+def calibrate_eps(s: MixStream, n_query: int = 3000, tol: float = 0.01, max_evals: int = 8) -> MixStream:
+    """The stream with Eps fitted so that the mean neighbour count (self
+    included, FP64 distances) of a seeded sample of its first window is
+    within `tol` of its target (clamped to [10.5, 29.5], leaving room for the
+    sampling error: with 3,000 sampled points every stream of the 256-stream
+    mix lands within 4% of its target over its whole window).  Secant steps on log(count)
+    against log(Eps), starting from the density estimate."""
+    from dataclasses import replace
+
+    from scipy.spatial import cKDTree
+
+    target = float(np.clip(s.target if s.target > 0 else 20.0, 10.5, 29.5))
+    win = mix_points(s, s.window).astype(np.float64)
+    tree = cKDTree(win, balanced_tree=False, compact_nodes=False)
+    rng = np.random.default_rng(s.seed)
+    q = win[rng.choice(len(win), size=min(n_query, len(win)), replace=False)]
+
+    def mean(e: float) -> float:
+        return float(np.mean(tree.query_ball_point(q, r=e, return_length=True)))
+
+    e0 = s.eps
+    m0 = mean(e0)
+    e1 = e0 * (target / m0) ** (1.0 / s.dim)
+    m1 = mean(e1)
+    for _ in range(max_evals - 2):
+        if abs(m1 - target) <= tol * target:
+            break
+        p = np.log(m1 / m0) / np.log(e1 / e0) if m1 != m0 and e1 != e0 else float(s.dim)
+        p = float(np.clip(p, 0.5, 4.0))
+        e0, m0 = e1, m1
+        e1 = e1 * (target / m1) ** (1.0 / p)
+        m1 = mean(e1)
+    return replace(s, eps=float(e1))
 
 
 def mix_points(s: MixStream, n_total: int) -> np.ndarray:
