@@ -241,7 +241,8 @@ RTDBS_API int rtdbs_get_stats(rtdbs_engine* engine, rtdbs_stats* stats);
  * work overlaps on a GPU race and corrupt each other's results, so serialise
  * them.  Runs on cuda_stream (a cudaStream_t, NULL = default stream) and
  * waits for that stream twice (for the points' bounding box, and at the end),
- * so it must not be called while the stream is being captured into a graph.
+ * so it must not be called while the stream is being captured into a graph
+ * (rtdbs_cluster_window_noalloc_async below waits for nothing).
  * Returns RTDBS_ERR_INVALID for n above the limit or bad arguments,
  * RTDBS_ERR_CUDA if a runtime call fails and RTDBS_ERR_DEVICE if a device-side
  * bound was hit, with the text in rtdbs_last_error; an error return comes
@@ -249,6 +250,24 @@ RTDBS_API int rtdbs_get_stats(rtdbs_engine* engine, rtdbs_stats* stats);
 RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int32_t n, int32_t dim, double eps,
                                            int32_t min_pts, int32_t precision, int32_t* d_label,
                                            int32_t* d_cluster_id, void* cuda_stream);
+
+/* rtdbs_cluster_window_noalloc without any wait, for latency paths and CUDA
+ * graph capture: the caller gives the grid's box (box_min[dim], box_max[dim],
+ * host memory; points outside it fall into its edge cells and are still
+ * clustered exactly, a tight box just keeps the grid small) and a device int
+ * *d_status, which receives the device error bits (0: success; 1 table full,
+ * 2 union-find bound, 4 work list full, 8 chunk bookkeeping) in stream order.
+ * Everything is queued on cuda_stream and the call returns; the outputs and
+ * *d_status are ready when the stream reaches that point.  Calls share the
+ * scratch array with rtdbs_cluster_window_noalloc: serialise them (calls on
+ * one stream are).  Returns RTDBS_ERR_INVALID for bad arguments or an empty
+ * or non-finite box (before queueing anything) and RTDBS_ERR_CUDA if queueing
+ * fails, in which case work queued before the failure may still run. */
+RTDBS_API int rtdbs_cluster_window_noalloc_async(const float* d_points, int32_t n, int32_t dim, double eps,
+                                                 int32_t min_pts, int32_t precision, const float* box_min,
+                                                 const float* box_max, int32_t* d_label,
+                                                 int32_t* d_cluster_id, int32_t* d_status,
+                                                 void* cuda_stream);
 
 /* rtdbs_slide_async with every kernel launched directly and bracketed by CUDA
  * events; synchronous.  Results are identical to an ordinary slide. */

@@ -124,12 +124,9 @@ int scratch_for_current_device(unsigned char** out) {
     return RTDBS_OK;
 }
 
-}  // namespace
-
-extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int32_t n, int32_t dim,
-                                                      double eps, int32_t min_pts, int32_t precision,
-                                                      int32_t* d_label, int32_t* d_cluster_id,
-                                                      void* cuda_stream) {
+// Argument checks shared by both entry points.
+int check_args(const float* d_points, int n, int dim, double eps, int precision, const int32_t* d_label,
+               const int32_t* d_cluster_id) {
     using rtdbs::set_error;
     if (!d_points || !d_label || !d_cluster_id)
         return set_error(RTDBS_ERR_INVALID, "noalloc: points, label and cluster_id must not be NULL");
@@ -141,41 +138,14 @@ extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int
         return set_error(RTDBS_ERR_INVALID, "noalloc: eps must be finite and > 0");
     if (precision != RTDBS_PREC_FP64 && precision != RTDBS_PREC_FP32)
         return set_error(RTDBS_ERR_INVALID, "noalloc: unknown precision mode %d", precision);
-    if (n == 0) return RTDBS_OK;
-    unsigned char* base = nullptr;
-    int rc = scratch_for_current_device(&base);
-    if (rc != RTDBS_OK) return rc;
-    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    return RTDBS_OK;
+}
 
-    // Once work is queued on s, an error return first waits for it, so that
-    // an error also means the scratch array is no longer in use.
-    bool queued = false;
-#define NOALLOC_TRY(expr)                                                                              \
-    do {                                                                                               \
-        const cudaError_t _e = (expr);                                                                 \
-        if (_e != cudaSuccess) {                                                                       \
-            if (queued) cudaStreamSynchronize(s);                                                      \
-            return set_error(RTDBS_ERR_CUDA, "noalloc: %s failed: %s", #expr, cudaGetErrorString(_e)); \
-        }                                                                                              \
-    } while (0)
-
-    // Every call reuses the array, which still holds the previous call's
-    // data: the cell tables (generation tags) and the control block must
-    // start at zero; everything else is rewritten before it is read.
-    queued = true;
-    NOALLOC_TRY(cudaMemsetAsync(base + kOffTable0, 0, sizeof(ulonglong2) * kTableSlots * 2, s));
-    NOALLOC_TRY(cudaMemsetAsync(base + kOffCtl, 0, sizeof(Ctl), s));
-
-    // Bounding box -> grid geometry (same rules as an engine without a box):
-    // the box comes back to the host, the one wait inside the call.
-    float* d_box = reinterpret_cast<float*>(base + kOffBox);
-    k_noalloc_bbox<<<1, 1024, 0, s>>>(d_points, n, dim, d_box);
-    NOALLOC_TRY(cudaGetLastError());
-    float box[6];
-    NOALLOC_TRY(cudaMemcpyAsync(box, d_box, sizeof(box), cudaMemcpyDeviceToHost, s));
-    NOALLOC_TRY(cudaStreamSynchronize(s));
-
-    View v;
+// The View of a window of n points in the scratch array at `base`, with the
+// grid over [bmin, bmax] (widened by 25% when `widen`).
+int window_view(View& v, unsigned char* base, const float* d_points, int n, int dim, double eps, int min_pts,
+                int precision, const float* bmin, const float* bmax, bool widen, int32_t* d_label,
+                int32_t* d_cluster_id) {
     std::memset(&v, 0, sizeof(v));
     v.dim = dim;
     v.cell_mult = 1;
@@ -188,8 +158,8 @@ extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int
     v.chunk = n;
     v.precision = precision;
     rtdbs::set_band(v, eps);
-    rc = rtdbs::set_geometry(v, dim, eps, 1, box, box + 3, true, nullptr);
-    if (rc != RTDBS_OK) return rc;  // nothing is queued after the wait above
+    const int rc = rtdbs::set_geometry(v, dim, eps, 1, bmin, bmax, widen, nullptr);
+    if (rc != RTDBS_OK) return rc;
     v.pbits = 15;
     v.pmask = (unsigned)(kTableSlots - 1);
     v.max_items = kMaxItems;
@@ -219,6 +189,63 @@ extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int
     v.xpt = reinterpret_cast<float4*>(base + kOffXpt);
     v.staging = d_points;  // the caller's points are read in place
     v.ctl = reinterpret_cast<Ctl*>(base + kOffCtl);
+    return RTDBS_OK;
+}
+
+// Every call reuses the array, which still holds the previous call's data:
+// the cell tables (generation tags) and the control block must start at
+// zero; everything else is rewritten before it is read.
+cudaError_t reset_scratch(unsigned char* base, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(base + kOffTable0, 0, sizeof(ulonglong2) * kTableSlots * 2, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(base + kOffCtl, 0, sizeof(Ctl), s);
+    return e;
+}
+
+}  // namespace
+
+extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int32_t n, int32_t dim,
+                                                      double eps, int32_t min_pts, int32_t precision,
+                                                      int32_t* d_label, int32_t* d_cluster_id,
+                                                      void* cuda_stream) {
+    using rtdbs::set_error;
+    int rc = check_args(d_points, n, dim, eps, precision, d_label, d_cluster_id);
+    if (rc != RTDBS_OK) return rc;
+    if (n == 0) return RTDBS_OK;
+    unsigned char* base = nullptr;
+    rc = scratch_for_current_device(&base);
+    if (rc != RTDBS_OK) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+
+    // Once work is queued on s, an error return first waits for it, so that
+    // an error also means the scratch array is no longer in use.
+    bool queued = false;
+#define NOALLOC_TRY(expr)                                                                              \
+    do {                                                                                               \
+        const cudaError_t _e = (expr);                                                                 \
+        if (_e != cudaSuccess) {                                                                       \
+            if (queued) cudaStreamSynchronize(s);                                                      \
+            return set_error(RTDBS_ERR_CUDA, "noalloc: %s failed: %s", #expr, cudaGetErrorString(_e)); \
+        }                                                                                              \
+    } while (0)
+
+    queued = true;
+    NOALLOC_TRY(reset_scratch(base, s));
+
+    // Bounding box -> grid geometry (same rules as an engine without a box):
+    // the box comes back to the host, the one wait inside the call
+    // (rtdbs_cluster_window_noalloc_async takes the box from the caller and
+    // does not wait at all).
+    float* d_box = reinterpret_cast<float*>(base + kOffBox);
+    k_noalloc_bbox<<<1, 1024, 0, s>>>(d_points, n, dim, d_box);
+    NOALLOC_TRY(cudaGetLastError());
+    float box[6];
+    NOALLOC_TRY(cudaMemcpyAsync(box, d_box, sizeof(box), cudaMemcpyDeviceToHost, s));
+    NOALLOC_TRY(cudaStreamSynchronize(s));
+
+    View v;
+    rc = window_view(v, base, d_points, n, dim, eps, min_pts, precision, box, box + 3, true, d_label,
+                     d_cluster_id);
+    if (rc != RTDBS_OK) return rc;  // nothing is queued after the wait above
 
     NOALLOC_TRY(rtdbs::launch_chunk_step(v, precision, 0, n, 1, 0, s));
     NOALLOC_TRY(rtdbs::launch_cluster(v, precision, 0, s));
@@ -229,5 +256,42 @@ extern "C" RTDBS_API int rtdbs_cluster_window_noalloc(const float* d_points, int
     if (err)
         return set_error(RTDBS_ERR_DEVICE, "noalloc: device error bits 0x%x (1 table full, 2 union-find bound, "
                          "4 work list full, 8 chunk bookkeeping)", err);
+    return RTDBS_OK;
+}
+
+extern "C" RTDBS_API int rtdbs_cluster_window_noalloc_async(const float* d_points, int32_t n, int32_t dim,
+                                                            double eps, int32_t min_pts, int32_t precision,
+                                                            const float* box_min, const float* box_max,
+                                                            int32_t* d_label, int32_t* d_cluster_id,
+                                                            int32_t* d_status, void* cuda_stream) {
+    using rtdbs::set_error;
+    int rc = check_args(d_points, n, dim, eps, precision, d_label, d_cluster_id);
+    if (rc != RTDBS_OK) return rc;
+    if (!box_min || !box_max || !d_status)
+        return set_error(RTDBS_ERR_INVALID, "noalloc: box_min, box_max and status must not be NULL");
+    unsigned char* base = nullptr;
+    rc = scratch_for_current_device(&base);
+    if (rc != RTDBS_OK) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    View v;
+    // geometry first: a bad box returns before anything is queued
+    rc = window_view(v, base, d_points, n > 0 ? n : 1, dim, eps, min_pts, precision, box_min, box_max, false,
+                     d_label, d_cluster_id);
+    if (rc != RTDBS_OK) return rc;
+#define NOALLOC_TRY(expr)                                                                              \
+    do {                                                                                               \
+        const cudaError_t _e = (expr);                                                                 \
+        if (_e != cudaSuccess)                                                                         \
+            return set_error(RTDBS_ERR_CUDA, "noalloc: %s failed: %s", #expr, cudaGetErrorString(_e)); \
+    } while (0)
+    if (n == 0) {
+        NOALLOC_TRY(cudaMemsetAsync(d_status, 0, sizeof(int32_t), s));
+        return RTDBS_OK;
+    }
+    NOALLOC_TRY(reset_scratch(base, s));
+    NOALLOC_TRY(rtdbs::launch_chunk_step(v, precision, 0, n, 1, 0, s));
+    NOALLOC_TRY(rtdbs::launch_cluster(v, precision, 0, s));
+    NOALLOC_TRY(cudaMemcpyAsync(d_status, &v.ctl->err, sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+#undef NOALLOC_TRY
     return RTDBS_OK;
 }

@@ -32,7 +32,7 @@ EXPORTED_SYMBOLS = (
     "rtdbs_create", "rtdbs_destroy", "rtdbs_load_window", "rtdbs_slide", "rtdbs_slide_async",
     "rtdbs_slide_pipelined",
     "rtdbs_sync", "rtdbs_cluster", "rtdbs_get_counts", "rtdbs_device_outputs", "rtdbs_get_stats",
-    "rtdbs_slide_profiled", "rtdbs_cluster_window_noalloc",
+    "rtdbs_slide_profiled", "rtdbs_cluster_window_noalloc", "rtdbs_cluster_window_noalloc_async",
     "rtdbs_stream_bytes", "rtdbs_pool_params_init", "rtdbs_pool_create", "rtdbs_pool_destroy",
     "rtdbs_pool_add_stream", "rtdbs_pool_remove_stream", "rtdbs_pool_load_window", "rtdbs_pool_slide",
     "rtdbs_pool_sync", "rtdbs_pool_outputs", "rtdbs_pool_read_outputs", "rtdbs_pool_engine",

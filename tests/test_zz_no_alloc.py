@@ -7,8 +7,10 @@ Called through the C ABI and compared bit-exactly with the allocating entry
 points (rtdbs_load_window + rtdbs_cluster) and with the CPU oracle on two
 calls in a row, with another window clustered in between.  Also checks that a
 warm call leaves the device's free memory unchanged, and that a call works as
-the first kernel launch of a fresh process.  This file is collected last on
-purpose.
+the first kernel launch of a fresh process.  The variant without waits
+(rtdbs_cluster_window_noalloc_async) is compared with the oracle with a box
+around and a box inside the data, and replayed from a captured CUDA graph on
+new points.  This file is collected last on purpose.
 """
 import ctypes
 import os
@@ -154,3 +156,90 @@ def test_noalloc_rejects_oversized_window(noalloc):
     rc = noalloc(d.data_ptr(), n, 2, 0.5, 4, E.PREC_FP64, out.data_ptr(), out.data_ptr(), None)
     assert rc == E.RTDBS_ERR_INVALID
     assert b"RTDBS_NOALLOC_MAX_POINTS" in E.load_library().rtdbs_last_error()
+
+
+# ---------------------------------------------------------------- no waits
+@pytest.fixture(scope="module")
+def noalloc_async(noalloc):
+    fn = E.load_library().rtdbs_cluster_window_noalloc_async
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_int32,
+                   ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                   ctypes.c_void_p, ctypes.c_void_p]
+    return fn
+
+
+def call_async(fn, bufs, dim, eps, mp, precision, lo, hi, status, stream):
+    d, lab, cid = bufs
+    blo = (ctypes.c_float * 3)(*[float(x) for x in lo])
+    bhi = (ctypes.c_float * 3)(*[float(x) for x in hi])
+    return fn(d.data_ptr(), d.shape[0], dim, float(eps), int(mp),
+              E.PREC_FP64 if precision == "fp64" else E.PREC_FP32, blo, bhi, lab.data_ptr(), cid.data_ptr(),
+              status.data_ptr(), stream)
+
+
+@pytest.mark.parametrize("shrink", [0.0, 0.3], ids=["data_box", "box_inside_data"])
+@pytest.mark.parametrize("name,gen,eps,mp,precision", CASES[:3], ids=[c[0] for c in CASES[:3]])
+def test_noalloc_async_matches_oracle(noalloc_async, name, gen, eps, mp, precision, shrink):
+    """The caller's box sets the grid; with a box inside the data (points
+    beyond it fall into the edge cells) the result is still exact."""
+    import torch
+
+    pts = gen()
+    mode = O.MODE_FP64 if precision == "fp64" else O.MODE_FP32
+    _, o_lab, o_cid, _ = O.window_grid(pts, eps, mp, mode)
+    lo, hi = pts.min(axis=0).astype(np.float64), pts.max(axis=0).astype(np.float64)
+    lo, hi = lo + shrink * (hi - lo), hi - shrink * (hi - lo)
+    bufs = device_buffers(pts)
+    status = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    rc = call_async(noalloc_async, bufs, pts.shape[1], eps, mp, precision, lo, hi, status,
+                    torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, E.load_library().rtdbs_last_error()
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    assert np.array_equal(bufs[1].cpu().numpy(), o_lab), f"{name}: labels differ from the oracle"
+    assert np.array_equal(bufs[2].cpu().numpy(), o_cid), f"{name}: ids differ from the oracle"
+
+
+def test_noalloc_async_captured_in_a_cuda_graph(noalloc_async):
+    """Captured once, replayed on new points written into the same input
+    buffer: every replay equals the oracle on the points it saw."""
+    import torch
+
+    n, eps, mp = 6_000, 0.5, 5
+    sets = [wl.gaussian_mixture(n, dim=2, k=8, box=25.0, seed=s) for s in (51, 52, 53)]
+    lo, hi = np.zeros(3), np.full(3, 25.0)
+    bufs = device_buffers(sets[0])
+    status = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):  # first call outside the capture (device set-up)
+        assert call_async(noalloc_async, bufs, 2, eps, mp, "fp64", lo, hi, status, side.cuda_stream) == 0
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        rc = call_async(noalloc_async, bufs, 2, eps, mp, "fp64", lo, hi, status,
+                        torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, E.load_library().rtdbs_last_error()
+    for pts in sets[1:] + sets[:1]:
+        bufs[0].copy_(torch.from_numpy(pts))
+        status.fill_(-1)
+        g.replay()
+        torch.cuda.synchronize()
+        _, o_lab, o_cid, _ = O.window_grid(pts, eps, mp, O.MODE_FP64)
+        assert int(status.item()) == 0
+        assert np.array_equal(bufs[1].cpu().numpy(), o_lab) and np.array_equal(bufs[2].cpu().numpy(), o_cid)
+
+
+def test_noalloc_async_rejects_bad_box_before_queueing(noalloc_async):
+    import torch
+
+    pts = wl.gaussian_mixture(1_000, dim=2, k=3, box=10.0, seed=54)
+    bufs = device_buffers(pts)
+    status = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    rc = call_async(noalloc_async, bufs, 2, 0.5, 4, "fp64", [5.0, 0.0, 0.0], [1.0, 10.0, 0.0], status, None)
+    assert rc == E.RTDBS_ERR_INVALID
+    torch.cuda.synchronize()
+    assert int(status.item()) == -1  # nothing was queued
+    assert np.all(bufs[1].cpu().numpy() == -7)
