@@ -215,7 +215,7 @@ def mix_eps(W: int, dim: int, box: float, target: float, k: int = 20, sigma: flo
 def calibrate_eps(s: MixStream, n_query: int = 3000, tol: float = 0.01, max_evals: int = 8) -> MixStream:
     """The stream with Eps fitted so that the mean neighbour count (self
     included, FP64 distances) of a seeded sample of its first window is
-    within `tol` of its target (clamped to [10.5, 29.5], leaving room for the
+    within `tol` of its target (clamped to [11, 29], leaving room for the
     sampling error: with 3,000 sampled points every stream of the 256-stream
     mix lands within 4% of its target over its whole window).  Secant steps on log(count)
     against log(Eps), starting from the density estimate."""
@@ -223,7 +223,7 @@ def calibrate_eps(s: MixStream, n_query: int = 3000, tol: float = 0.01, max_eval
 
     from scipy.spatial import cKDTree
 
-    target = float(np.clip(s.target if s.target > 0 else 20.0, 10.5, 29.5))
+    target = float(np.clip(s.target if s.target > 0 else 20.0, 11.0, 29.0))
     win = mix_points(s, s.window).astype(np.float64)
     tree = cKDTree(win, balanced_tree=False, compact_nodes=False)
     rng = np.random.default_rng(s.seed)
@@ -247,5 +247,18 @@ def calibrate_eps(s: MixStream, n_query: int = 3000, tol: float = 0.01, max_eval
     return replace(s, eps=float(e1))
 
 
-def mix_points(s: MixStream, n_total: int) -> np.ndarray:
-    return gaussian_mixture(n_total, dim=s.dim, k=20, box=s.box, sigma=1.0, seed=s.seed)
+def mix_points(s: MixStream, n_total: int, k: int = 20, block: int = 4096) -> np.ndarray:
+    """The stream's first n_total points: k Gaussians (sigma 1, centres
+    uniform in the box) with 10% uniform noise, drawn in blocks of `block`
+    points from per-block seeds, so a stream's first points do not depend on
+    how many are drawn (the window Eps is fitted on is the window the
+    benchmarks slide from)."""
+    centres = np.random.default_rng(s.seed).uniform(0.0, s.box, size=(k, s.dim))
+    out = np.empty((-(-n_total // block) * block, s.dim), np.float64)
+    for b in range(len(out) // block):
+        r = np.random.default_rng([s.seed, b])
+        blk = centres[r.integers(0, k, size=block)] + r.normal(0.0, 1.0, size=(block, s.dim))
+        noise = r.random(block) < 0.10
+        blk[noise] = r.uniform(0.0, s.box, size=(int(noise.sum()), s.dim))
+        out[b * block:(b + 1) * block] = blk
+    return out[:n_total].astype(np.float32)
