@@ -232,11 +232,11 @@ RTDBS_API int rtdbs_get_stats(rtdbs_engine* engine, rtdbs_stats* stats);
  * memory in its own pool and forbids raw allocations by plug-ins, or a caller
  * on a latency path that cannot take cudaMalloc's implicit synchronisation).
  * Inputs and outputs are device memory owned by the caller: d_points[n][dim],
- * d_label[n], d_cluster_id[n] (index = the point's position in d_points, with
- * the same labels and ids as rtdbs_load_window + rtdbs_cluster on a window of
- * n slots).  Working memory is one static device array of about 3.4 MB,
- * part of the library: every GPU that loads the library holds it until the
- * process exits.  The first call on a device looks up that array's device
+ * d_label[n], d_cluster_id[n] (NULL allowed when n = 0; index = the point's
+ * position in d_points, with the same labels and ids as rtdbs_load_window +
+ * rtdbs_cluster on a window of n slots).  Working memory is one static
+ * device array of about 3.4 MB, part of the library: every GPU that loads the
+ * library holds it until the process exits.  The first call on a device looks up that array's device
  * address, with that device current.  All calls share the array: calls whose
  * work overlaps on a GPU race and corrupt each other's results, so serialise
  * them.  Runs on cuda_stream (a cudaStream_t, NULL = default stream) and

@@ -128,7 +128,7 @@ int scratch_for_current_device(unsigned char** out) {
 int check_args(const float* d_points, int n, int dim, double eps, int precision, const int32_t* d_label,
                const int32_t* d_cluster_id) {
     using rtdbs::set_error;
-    if (!d_points || !d_label || !d_cluster_id)
+    if (n > 0 && (!d_points || !d_label || !d_cluster_id))  // (an empty window touches none of them)
         return set_error(RTDBS_ERR_INVALID, "noalloc: points, label and cluster_id must not be NULL");
     if (n < 0 || n > kMaxPoints)  // beyond the scratch array
         return set_error(RTDBS_ERR_INVALID, "noalloc: n = %d outside 0..%d (RTDBS_NOALLOC_MAX_POINTS)", n,

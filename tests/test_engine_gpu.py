@@ -379,13 +379,18 @@ def test_two_cells_per_eps_match_oracle(name, gen, W, S, eps, mp, slides, precis
     assert_same(got[:3], exp, f"{name}/{precision}/K2")
 
 
-# Edge shapes: one-point strides, tiny windows, MinPts 1 (every point core)
-# and 2 (empty neighbour lists), duplicates at one location, 1-D.
+# Edge shapes: one-point strides, tiny windows (down to one slot), MinPts 1
+# (every point core) and 2 (empty neighbour lists), duplicates at one
+# location, 1-D.
 EDGE_CASES = [
     ("S1_W64_2d", lambda: wl.gaussian_mixture(64 + 40, dim=2, k=2, box=3.0, seed=41), 64, 1, 0.5, 4),
     ("mp1_3d", lambda: wl.gaussian_mixture(2_000 + 3 * 200, dim=3, k=4, box=10.0, seed=42), 2_000, 200, 0.8, 1),
     ("mp2_2d", lambda: wl.gaussian_mixture(2_000 + 3 * 200, dim=2, k=4, box=40.0, seed=43), 2_000, 200, 0.3, 2),
     ("dups_1d", lambda: np.repeat(np.linspace(0, 5, 300, dtype=np.float32)[:, None], 4, axis=0), 800, 100, 0.02, 5),
+    # the smallest windows: one slot, two slots with MinPts 2, one chunk of three 1-D points
+    ("W1_S1_2d", lambda: wl.gaussian_mixture(1 + 30, dim=2, k=2, box=2.0, seed=71), 1, 1, 0.5, 1),
+    ("W2_S1_3d", lambda: wl.gaussian_mixture(2 + 30, dim=3, k=2, box=2.0, seed=72), 2, 1, 0.5, 2),
+    ("W3_S3_1d", lambda: wl.gaussian_mixture(3 + 30, dim=1, k=2, box=2.0, seed=73), 3, 3, 0.5, 2),
 ]
 
 

@@ -232,6 +232,28 @@ def test_noalloc_async_captured_in_a_cuda_graph(noalloc_async):
         assert np.array_equal(bufs[1].cpu().numpy(), o_lab) and np.array_equal(bufs[2].cpu().numpy(), o_cid)
 
 
+def test_noalloc_tiny_windows(noalloc, noalloc_async):
+    """One point (a core with MinPts 1, noise with 2) and an empty window."""
+    import torch
+
+    pts = np.array([[0.25, -1.5]], np.float32)
+    for mp, lab in ((1, 0), (2, 2)):
+        got_lab, got_cid = call_noalloc(noalloc, pts, 0.5, mp, "fp64")
+        assert got_lab.tolist() == [lab] and got_cid.tolist() == [0]
+        bufs = device_buffers(pts)
+        status = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+        assert call_async(noalloc_async, bufs, 2, 0.5, mp, "fp64", pts[0], pts[0], status, None) == 0
+        torch.cuda.synchronize()
+        assert int(status.item()) == 0
+        assert bufs[1].cpu().tolist() == [lab] and bufs[2].cpu().tolist() == [0]
+    empty = torch.empty((0, 2), dtype=torch.float32, device="cuda")
+    out = torch.empty(1, dtype=torch.int32, device="cuda")
+    status = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    assert call_async(noalloc_async, (empty, out, out), 2, 0.5, 2, "fp64", [0, 0], [1, 1], status, None) == 0
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+
+
 def test_noalloc_async_rejects_bad_box_before_queueing(noalloc_async):
     import torch
 
