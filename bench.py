@@ -554,7 +554,8 @@ def run_cfg0(args, dev, stream) -> dict:
     MinPts 5) in the reference's FP32 predicate: every slide's counts, labels
     and ids compared with the reference's CPU path, which is timed on every
     slide.  Device-resident slides timed with CUDA events, then the same
-    stream end to end through rtdbs_slide with host buffers."""
+    stream end to end through rtdbs_slide with host buffers, and through
+    rtdbs_slide_pipelined (one slide in flight)."""
     import torch
 
     from rtdbstream_gb300 import Engine
@@ -595,6 +596,24 @@ def run_cfg0(args, dev, stream) -> dict:
         if not (np.array_equal(h_lab, elab) and np.array_equal(h_cid, ecid) and np.array_equal(eng.counts(), enn)):
             bad.append(k + 1)
     eng.close()
+    # end to end with one slide in flight (rtdbs_slide_pipelined): pinned input
+    # stride, two pinned output sets used in turn; host wall clock over all
+    # slides and the final sync; the last slide's outputs checked
+    eng = Engine(2, sp.window, sp.stride, sp.eps, sp.min_pts, precision="fp32", device=dev,
+                 stream=stream.cuda_stream)
+    eng.load_window(pts[:sp.window])
+    p_pts = torch.from_numpy(pts).pin_memory().numpy()
+    outs = [tuple(torch.empty(sp.window, dtype=torch.int32).pin_memory().numpy() for _ in range(2))
+            for _ in range(2)]
+    t0 = time.perf_counter()
+    for k in range(sp.slides):
+        eng.slide_pipelined(p_pts[sp.window + k * sp.stride: sp.window + (k + 1) * sp.stride], *outs[k % 2])
+    eng.sync()
+    pipe_s = time.perf_counter() - t0
+    _, elab, ecid = ref[sp.slides]
+    last_lab, last_cid = outs[(sp.slides - 1) % 2]
+    pipe_exact = bool(np.array_equal(last_lab, elab) and np.array_equal(last_cid, ecid))
+    eng.close()
     gpu_value = sp.slides * sp.stride / (sum(per_ms) / 1000.0)
     return {"workload": f"2-D mixture W={sp.window:,} S={sp.stride:,} Eps={sp.eps} MinPts={sp.min_pts}, "
                         f"{sp.slides} slides, fp32 (the reference's predicate)",
@@ -603,6 +622,9 @@ def run_cfg0(args, dev, stream) -> dict:
             "e2e": {"value": sp.slides * sp.stride / sum(e2e_s), "unit": UNIT,
                     "latency_ms_p50": 1000 * float(np.percentile(e2e_s, 50)),
                     "latency_ms_p99": 1000 * float(np.percentile(e2e_s, 99))},
+            "e2e_pipelined": {"value": sp.slides * sp.stride / pipe_s, "unit": UNIT,
+                              "api": "rtdbs_slide_pipelined, pinned host buffers, one slide in flight",
+                              "last_slide_exact": pipe_exact},
             "cpu_reference": cpu,
             "e2e_vs_cpu_reference": sp.slides * sp.stride / sum(e2e_s) / cpu["slid_points_per_s"],
             "slides_exact_vs_reference_cpu": sp.slides - len(bad), "slides_differing": bad}
