@@ -39,7 +39,7 @@ import numpy as np
 from .engine import Engine, make_params
 
 # (cell_mult, work_grab, query_lanes); the first is the default
-CANDIDATES: Tuple[Tuple[int, int, int], ...] = ((1, 8, 16), (1, 4, 16), (1, 16, 16), (1, 2, 16), (1, 1, 16),
+CANDIDATES: Tuple[Tuple[int, int, int], ...] = ((1, 8, 16), (1, 5, 16), (1, 4, 16), (1, 16, 16), (1, 2, 16), (1, 1, 16),
                                                 (1, 8, 32), (2, 8, 32), (2, 4, 32), (2, 16, 32), (2, 1, 32))
 MARGIN = 0.97           # a candidate replaces the default only when this much faster
 POOL_STREAMS = 16       # streams of a bucket timed together by choose_batched

@@ -45,6 +45,7 @@ constexpr int kSortRun = 1024;     // words per radix-sort CTA (one per thread)
 constexpr int kBuildThreads = 512;
 constexpr int kClusterThreads = 256;
 constexpr int kBatch = 8;          // default work items a clustering warp takes at a time
+                                   // in a pool launch
 constexpr int kQueryLanes = 16;    // default lanes per query point in the count passes (one
                                    // cell per Eps: two points per warp overlap their loads)
 constexpr int kMaxIter = 1 << 20;  // bound on every device-side retry loop
@@ -94,7 +95,8 @@ struct View {
     int dim;
     int cell_mult;              // K: cells per Eps along each axis (1 or 2)
     int grab;                   // work items a clustering warp takes from the queue at a time
-                                // (0: 8 in pool launches, fewer on small single windows)
+                                // (0: 8 in pool launches; for a window slid alone 5, fewer
+                                // on small ones)
     int qlanes;                 // lanes per query point in the count passes (16 or 32)
     // parameters
     int W, S, min_pts, units;   // units = W / S

@@ -1394,6 +1394,8 @@ __global__ void k_hints(View v) {
 // from per-position root hints.  Each warp walks
 // a contiguous range of work items (neighbouring cells), so candidate loads
 // reuse L1.
+constexpr int kSingleGrab = 5;  // default work items per grab of a large window slid alone
+
 struct ClusterSmem {
     int home_root[kClusterThreads / 32][32];
     float4 home_pt[kClusterThreads / 32][32];
@@ -1401,12 +1403,13 @@ struct ClusterSmem {
 };
 
 // Work items a warp takes at a time: the stream's setting, or by default 8
-// in a pool launch (many streams share the GPU) and for a single stream 8 on
-// large windows, fewer on small ones (a 10k-point window has a few hundred to
-// a few thousand items: 8 per grab would leave them to a few dozen warps).
+// in a pool launch (many streams share the GPU) and for a single stream 5 on
+// large windows (a 1M-point walker window: union 233 us with 8, 224 with 5),
+// fewer on small ones (a 10k-point window has a few hundred to a few
+// thousand items: 5 per grab would leave them to a few dozen warps).
 __device__ __forceinline__ int work_grab(const View& v, bool pooled) {
     if (v.grab > 0) return v.grab;
-    return pooled ? kBatch : max(1, min(kBatch, v.W >> 14));
+    return pooled ? kBatch : max(1, min(kSingleGrab, v.W >> 14));
 }
 
 template <int MODE, int DK>
