@@ -94,9 +94,10 @@ typedef struct rtdbs_params {
                              (src/dbscan/dbscan.cpp:34-37) */
     int32_t work_grab;    /* work items (cell runs) a clustering warp takes from the shared
                              queue at a time, 1..64 (0 = 8 in a pool; for a stream slid on
-                             its own, 5 on large windows and fewer on small ones: 1 below
-                             32,768 points): the work split between warps, picked by
-                             rtdbstream_gb300/autotune.py.  No reference counterpart */
+                             its own, 5 or 8 on large windows by cell occupancy and fewer
+                             on small ones: 1 below 32,768 points): the work split between
+                             warps, picked by rtdbstream_gb300/autotune.py.  No reference
+                             counterpart */
     int32_t query_lanes;  /* lanes that scan one expired or new point's neighbourhood in the
                              count passes, 16 or 32 (0 = 16 with one cell per Eps, 32 with
                              two; two cells per Eps needs 32): the block shape of those

@@ -95,8 +95,8 @@ struct View {
     int dim;
     int cell_mult;              // K: cells per Eps along each axis (1 or 2)
     int grab;                   // work items a clustering warp takes from the queue at a time
-                                // (0: 8 in pool launches; for a window slid alone 5, fewer
-                                // on small ones)
+                                // (0: 8 in pool launches; for a large window slid alone 5
+                                // or 8 by items per point, fewer on small ones)
     int qlanes;                 // lanes per query point in the count passes (16 or 32)
     // parameters
     int W, S, min_pts, units;   // units = W / S

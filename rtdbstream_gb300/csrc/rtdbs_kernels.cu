@@ -1395,6 +1395,7 @@ __global__ void k_hints(View v) {
 // a contiguous range of work items (neighbouring cells), so candidate loads
 // reuse L1.
 constexpr int kSingleGrab = 5;  // default work items per grab of a large window slid alone
+                                // whose cells hold several points
 
 struct ClusterSmem {
     int home_root[kClusterThreads / 32][32];
@@ -1403,13 +1404,20 @@ struct ClusterSmem {
 };
 
 // Work items a warp takes at a time: the stream's setting, or by default 8
-// in a pool launch (many streams share the GPU) and for a single stream 5 on
-// large windows (a 1M-point walker window: union 233 us with 8, 224 with 5),
-// fewer on small ones (a 10k-point window has a few hundred to a few
-// thousand items: 5 per grab would leave them to a few dozen warps).
+// in a pool launch (many streams share the GPU); for a single stream up to 8
+// on large windows, fewer on small ones (a 10k-point window has a few hundred
+// to a few thousand items: 8 per grab would leave them to a few dozen warps),
+// and 5 where cells hold several points (fewer than 0.4 items per window
+// point): items are then costly enough that balance beats the queue's atomics
+// (a 1M-point walker window, 0.3 items per point: union 233 us with 8, 224
+// with 5), where on windows of near-empty cells (one item per point, most of
+// them without a core) the atomics dominate and 8 stays faster.
 __device__ __forceinline__ int work_grab(const View& v, bool pooled) {
     if (v.grab > 0) return v.grab;
-    return pooled ? kBatch : max(1, min(kSingleGrab, v.W >> 14));
+    if (pooled) return kBatch;
+    const int g = max(1, min(kBatch, v.W >> 14));
+    const long long items = v.ctl->nitems;
+    return (g > kSingleGrab && items * 5 < (long long)v.W * 2) ? kSingleGrab : g;
 }
 
 template <int MODE, int DK>
