@@ -251,8 +251,9 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int):
+    def __init__(self, gpu_index: int, interval_ms: int = 20):
         self.gpu = gpu_index
+        self.interval_ms = interval_ms
         self.proc = None
         self.lines = []
 
@@ -260,10 +261,15 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.interval_ms)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # the sampler is live (its first sample is in) before the timed work starts
+            t_end = time.time() + 5.0
+            while not self.lines and self.proc.poll() is None and time.time() < t_end:
+                time.sleep(0.005)
+            self.lines.clear()
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -407,15 +413,16 @@ def run_ours(args) -> None:
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(dev) as clk:
-        for k in range(args.steps):
-            flush.fill_(float(k))
-            starts[k].record(stream)
-            eng.slide_async(new_pts(step))
-            ends[k].record(stream)
-            step += 1
-        eng.sync()
-        torch.cuda.synchronize()
+    # clocks sampled over the timed loops (device-resident, then end to end)
+    clk = ClockSampler(dev).__enter__()
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        starts[k].record(stream)
+        eng.slide_async(new_pts(step))
+        ends[k].record(stream)
+        step += 1
+    eng.sync()
+    torch.cuda.synchronize()
     per_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     value, total_ms = weak_scaling_value(float(sum(per_ms)), args.steps, S, world, f"cuda:{dev}")
 
@@ -447,6 +454,7 @@ def run_ours(args) -> None:
             step += 1
         eng.sync()
         e2e_value = S * args.e2e_steps / (time.perf_counter() - t0)
+    clk.__exit__(None, None, None)
 
     # per-phase device times (direct launches bracketed by events) and the
     # counters of the same slides
