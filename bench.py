@@ -369,6 +369,43 @@ def ncu_traffic(phase: str):
         return None
 
 
+def headline_summary(line: dict) -> dict:
+    """The line's headline figures, rounded, in a few hundred characters:
+    printed as the line's last key so that a reader keeping only the end of
+    the output still has them (the full blocks stay above)."""
+    def r(x, n=3):
+        return None if x is None else float(f"{x:.{n}g}")
+
+    out = {"walker": {"ms_per_slide": r(line.get("ms_per_step"), 4), "value": r(line.get("value")),
+                      "e2e_pipelined": r((line.get("e2e") or {}).get("value")),
+                      "e2e_synchronous": r(((line.get("e2e") or {}).get("synchronous") or {}).get("value")),
+                      "exact_vs_fp64_oracle": line.get("exact_vs_fp64_oracle"),
+                      "union_roofline_frac": r((line.get("roofline") or {}).get("frac"))}}
+    c0 = line.get("cfg0")
+    if c0:
+        out["cfg0"] = {"value": r(c0["value"]), "e2e": r(c0["e2e"]["value"]),
+                       "e2e_pipelined": r(c0["e2e_pipelined"]["value"]),
+                       "slides_exact_vs_reference_cpu": c0["slides_exact_vs_reference_cpu"],
+                       "cpu_reference": r(c0["cpu_reference"]["slid_points_per_s"])}
+    c2 = line.get("cfg2")
+    if c2:
+        out["cfg2"] = {"value": r(c2["value"]), "rechecked_pairs_per_slide": c2["rechecked_pairs_per_slide"],
+                       "mismatches_vs_fp64_oracle": c2["mismatches_vs_fp64_oracle"]}
+    b = line.get("batched")
+    if b:
+        out["batched"] = {"value": r(b["value"]), "round_ms_p50": r(b["round_ms_p50"]),
+                          "speedup_vs_tuned_plain": r(b["speedup_vs_plain"]),
+                          "speedup_vs_fixed_plain": r(b["value"] / b["plain_one_at_a_time_default"]["value"]),
+                          "streams_exact_vs_fp64_oracle": b["streams_exact_vs_fp64_oracle"]}
+    sv = line.get("serving")
+    if sv:
+        out["serving"] = {"capacity_requests_per_s": r(sv["capacity_requests_per_s"]),
+                          "p50_p99_ms_by_load": {str(e["offered_fraction"]): [r(e["latency_ms_p50"]),
+                                                                               r(e["latency_ms_p99"])]
+                                                 for e in sv["sweep"]}}
+    return out
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -521,6 +558,7 @@ def run_ours(args) -> None:
     if not args.no_serving:
         line["serving"] = run_serving(args, dev, stream, world, rank)
     if rank == 0:
+        line["summary"] = headline_summary(line)  # last: the line's tail carries the headline figures
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
