@@ -558,7 +558,10 @@ def run_ours(args) -> None:
     if not args.no_serving:
         line["serving"] = run_serving(args, dev, stream, world, rank)
     if rank == 0:
-        line["summary"] = headline_summary(line)  # last: the line's tail carries the headline figures
+        try:
+            line["summary"] = headline_summary(line)  # last: the line's tail carries the headline figures
+        except (KeyError, TypeError, ValueError) as e:  # a missing figure must not cost the line
+            print(f"bench: no summary ({e!r})", file=sys.stderr)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
